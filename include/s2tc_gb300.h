@@ -1,0 +1,122 @@
+/*
+ * s2tc_gb300.h -- C ABI of the GB300 S2TC encoder library (libs2tc_gb300.so).
+ *
+ * Part 1 is a drop-in for the reference's libtxc_dxtn plugin ABI and encoder
+ * API: same symbol names, argument meaning, environment knobs, output bytes
+ * and error behaviour.  Part 2 is the GPU extension (device pointers, streams,
+ * batches, status codes).  All types are plain C; no CUDA or GL header is
+ * needed to include this file (GLint = int, GLubyte = unsigned char,
+ * GLenum = unsigned int, GLvoid = void, as in <GL/gl.h>).
+ */
+#ifndef S2TC_GB300_H
+#define S2TC_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------
+ * Part 1: reference-compatible entry points
+ * ------------------------------------------------------------------------ */
+
+/* GL_EXT_texture_compression_s3tc format enums accepted as `destformat`. */
+#define S2TC_GL_COMPRESSED_RGB_S3TC_DXT1_EXT  0x83F0
+#define S2TC_GL_COMPRESSED_RGBA_S3TC_DXT1_EXT 0x83F1
+#define S2TC_GL_COMPRESSED_RGBA_S3TC_DXT3_EXT 0x83F2
+#define S2TC_GL_COMPRESSED_RGBA_S3TC_DXT5_EXT 0x83F3
+
+/* Enums with the reference's values (s2tc_algorithm.h:31-63). */
+typedef enum { DITHER_NONE, DITHER_SIMPLE, DITHER_FLOYDSTEINBERG } DitherMode;
+typedef enum { DXT1, DXT3, DXT5 } DxtMode;
+typedef enum { REFINE_NEVER, REFINE_ALWAYS, REFINE_LOOP } RefinementMode;
+typedef enum { RGB, YUV, SRGB, SRGB_MIXED, AVG, WAVG, W0AVG, NORMALMAP } ColorDistMode;
+
+/* Compress a packed RGB8 (srccomps 3) or RGBA8 (any other srccomps) image of
+ * width x height texels from host memory into S2TC DXT1/DXT3/DXT5 blocks at
+ * `dest`, block rows dstRowStride bytes apart when dstRowStride is at least
+ * the packed row size (else packed).  Reads S2TC_DITHER_MODE,
+ * S2TC_COLORDIST_MODE, S2TC_RANDOM_COLORS and S2TC_REFINE_COLORS on every
+ * call.  A bad format prints "libdxtn: Bad dstFormat ..." and writes
+ * nothing.  The work runs on the GPU; the call returns when `dest` is written.
+ * Replaces: txc_dxtn.h:47-49, s2tc_libtxc_dxtn.cpp:142-299. */
+void tx_compress_dxtn(int srccomps, int width, int height, const unsigned char *srcPixData,
+		      unsigned int destformat, unsigned char *dest, int dstRowStride);
+
+/* Decode one texel (i, j) of a DXTn image whose rows are srcRowStride texels
+ * wide into RGB(A)8 `texel`.  Host functions (one texel per call).
+ * Replaces: txc_dxtn.h:38-45, s2tc_libtxc_dxtn.cpp:35-140. */
+void fetch_2d_texel_rgb_dxt1(int srcRowStride, const unsigned char *pixdata, int i, int j, void *texel);
+void fetch_2d_texel_rgba_dxt1(int srcRowStride, const unsigned char *pixdata, int i, int j, void *texel);
+void fetch_2d_texel_rgba_dxt3(int srcRowStride, const unsigned char *pixdata, int i, int j, void *texel);
+void fetch_2d_texel_rgba_dxt5(int srcRowStride, const unsigned char *pixdata, int i, int j, void *texel);
+
+/* Quantise a host RGB8/RGBA8 image to 4-byte texels (r 0..31, g 0..63,
+ * b 0..31, alpha with `alphabits` 1/4/8 bits) with the given dither, on the GPU.
+ * Replaces: s2tc_algorithm.h:38, s2tc_algorithm.cpp:1453-1465. */
+void rgb565_image(unsigned char *out, const unsigned char *rgba, int w, int h, int srccomps, int alphabits,
+		  DitherMode dither);
+
+/* Per-block encoder selected by format, metric, candidate count and
+ * refinement, as in the reference; the returned function encodes one block of
+ * a host 4-byte texel buffer (row length iw) and runs it on the GPU, one
+ * launch per call (a compatibility path: batch through tx_compress_dxtn or the
+ * extension API for throughput).
+ * Replaces: s2tc_algorithm.h:65-66, s2tc_algorithm.cpp:1164-1194. */
+typedef void (*s2tc_encode_block_func_t)(unsigned char *out, const unsigned char *rgba, int iw, int w, int h,
+					 int nrandom);
+s2tc_encode_block_func_t s2tc_encode_block_func(DxtMode dxt, ColorDistMode cd, int nrandom, RefinementMode refine);
+
+/* ------------------------------------------------------------------------
+ * Part 2: GPU extension API
+ * ------------------------------------------------------------------------ */
+
+/* Status codes. */
+#define S2TC_OK 0
+#define S2TC_ERR_ARGUMENT 1
+#define S2TC_ERR_FORMAT 2
+#define S2TC_ERR_CUDA 3
+#define S2TC_ERR_NOMEM 4
+#define S2TC_ERR_TIMEOUT 5
+#define S2TC_ERR_TOO_LARGE 6
+
+/* Encoder knobs with the meaning of the S2TC_* environment variables. */
+typedef struct s2tc_options {
+	int dither;  /* DitherMode */
+	int metric;  /* ColorDistMode */
+	int nrandom; /* S2TC_RANDOM_COLORS: <0 quick, 0 all texels, >0 extra random candidates */
+	int refine;  /* RefinementMode */
+} s2tc_options;
+
+/* Fill `opt` from the environment exactly as tx_compress_dxtn does (defaults
+ * SIMPLE / WAVG / -1 / ALWAYS; invalid values print the reference's message and
+ * keep the default). */
+void s2tc_options_from_env(s2tc_options *opt);
+
+/* Compress one image that already lives in device memory, on `stream` (a
+ * cudaStream_t, or NULL for the library's stream).  `d_dst` receives the
+ * blocks, block rows dst_pitch bytes apart.  For opt->nrandom > 0 the random
+ * candidates come from `d_rand` (nrandom*(3 or 4) rand() words per block in
+ * raster order) or, when d_rand is NULL, from libc rand() replayed on the
+ * host.  Scratch memory comes from the library's device arena.  Returns a
+ * status code; asynchronous with respect to the host unless rand() is
+ * replayed. */
+int s2tc_gpu_compress(int srccomps, int width, int height, const void *d_src, unsigned int destformat, void *d_dst,
+		      long long dst_pitch, const s2tc_options *opt, const unsigned int *d_rand, void *stream);
+
+/* Wait for `stream` (NULL: the library's stream) and report whether any
+ * kernel since the last check gave up a bounded wait (S2TC_ERR_TIMEOUT). */
+int s2tc_gpu_synchronize(void *stream);
+
+/* Number of rand() words an image consumes: blocks * nrandom * (4 for DXT5,
+ * else 3) when the random-candidate search is active, else 0. */
+long long s2tc_rand_words(int width, int height, unsigned int destformat, const s2tc_options *opt);
+
+/* Text of the last error this thread saw (empty when none). */
+const char *s2tc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,225 @@
+"""GB300 S2TC encoder: Python view of the C ABI in ``include/s2tc_gb300.h``.
+
+The compute path is ``libs2tc_gb300.so`` (hand-written CUDA for sm_103a behind a
+C ABI).  This module only loads it and converts numpy / torch buffers to
+pointers; it has no encoding code of its own, so there is nothing to fall back
+to: if the library cannot be loaded, importing ``lib`` raises.
+
+Names and argument meaning follow the reference's API (divVerent/s2tc:
+``tx_compress_dxtn`` in txc_dxtn.h:47-49, ``rgb565_image`` and
+``s2tc_encode_block_func`` in s2tc_algorithm.h:38, 65-66).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libs2tc_gb300.so"
+
+# GL_EXT_texture_compression_s3tc formats
+GL_COMPRESSED_RGB_S3TC_DXT1_EXT = 0x83F0
+GL_COMPRESSED_RGBA_S3TC_DXT1_EXT = 0x83F1
+GL_COMPRESSED_RGBA_S3TC_DXT3_EXT = 0x83F2
+GL_COMPRESSED_RGBA_S3TC_DXT5_EXT = 0x83F3
+FORMATS = (GL_COMPRESSED_RGB_S3TC_DXT1_EXT, GL_COMPRESSED_RGBA_S3TC_DXT1_EXT,
+           GL_COMPRESSED_RGBA_S3TC_DXT3_EXT, GL_COMPRESSED_RGBA_S3TC_DXT5_EXT)
+
+# Enums with the reference's values (s2tc_algorithm.h:31-63)
+DITHER_NONE, DITHER_SIMPLE, DITHER_FLOYDSTEINBERG = 0, 1, 2
+DXT1, DXT3, DXT5 = 0, 1, 2
+REFINE_NEVER, REFINE_ALWAYS, REFINE_LOOP = 0, 1, 2
+RGB, YUV, SRGB, SRGB_MIXED, AVG, WAVG, W0AVG, NORMALMAP = range(8)
+
+DITHER_NAMES = ("NONE", "SIMPLE", "FLOYDSTEINBERG")
+COLORDIST_NAMES = ("RGB", "YUV", "SRGB", "SRGB_MIXED", "AVG", "WAVG", "W0AVG", "NORMALMAP")
+REFINE_NAMES = ("NEVER", "ALWAYS", "LOOP")
+
+S2TC_OK = 0
+
+
+class S2tcError(RuntimeError):
+    pass
+
+
+class Options(ctypes.Structure):
+    """``s2tc_options``: the S2TC_* knobs as a struct."""
+    _fields_ = [("dither", ctypes.c_int), ("metric", ctypes.c_int),
+                ("nrandom", ctypes.c_int), ("refine", ctypes.c_int)]
+
+
+def format_dxt(fmt: int) -> int:
+    return {GL_COMPRESSED_RGB_S3TC_DXT1_EXT: DXT1, GL_COMPRESSED_RGBA_S3TC_DXT1_EXT: DXT1,
+            GL_COMPRESSED_RGBA_S3TC_DXT3_EXT: DXT3, GL_COMPRESSED_RGBA_S3TC_DXT5_EXT: DXT5}[fmt]
+
+
+def block_bytes(fmt: int) -> int:
+    return 8 if format_dxt(fmt) == DXT1 else 16
+
+
+def compressed_size(width: int, height: int, fmt: int) -> int:
+    return ((width + 3) // 4) * ((height + 3) // 4) * block_bytes(fmt)
+
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
+    """Load ``libs2tc_gb300.so`` (building is ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise S2tcError(f"{p} is missing: build it with s2tc_gb300/build.py")
+    lib = ctypes.CDLL(str(p))
+    c_int, c_uint, vp, c_ll = ctypes.c_int, ctypes.c_uint, ctypes.c_void_p, ctypes.c_longlong
+    lib.tx_compress_dxtn.argtypes = [c_int, c_int, c_int, vp, c_uint, vp, c_int]
+    lib.tx_compress_dxtn.restype = None
+    lib.rgb565_image.argtypes = [vp, vp, c_int, c_int, c_int, c_int, c_int]
+    lib.rgb565_image.restype = None
+    lib.s2tc_encode_block_func.argtypes = [c_int, c_int, c_int, c_int]
+    lib.s2tc_encode_block_func.restype = vp
+    for name in ("fetch_2d_texel_rgb_dxt1", "fetch_2d_texel_rgba_dxt1",
+                 "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5"):
+        f = getattr(lib, name)
+        f.argtypes = [c_int, vp, c_int, c_int, vp]
+        f.restype = None
+    lib.s2tc_options_from_env.argtypes = [ctypes.POINTER(Options)]
+    lib.s2tc_options_from_env.restype = None
+    lib.s2tc_gpu_compress.argtypes = [c_int, c_int, c_int, vp, c_uint, vp, c_ll,
+                                      ctypes.POINTER(Options), vp, vp]
+    lib.s2tc_gpu_compress.restype = c_int
+    lib.s2tc_gpu_synchronize.argtypes = [vp]
+    lib.s2tc_gpu_synchronize.restype = c_int
+    lib.s2tc_rand_words.argtypes = [c_int, c_int, c_uint, ctypes.POINTER(Options)]
+    lib.s2tc_rand_words.restype = c_ll
+    lib.s2tc_last_error.argtypes = []
+    lib.s2tc_last_error.restype = ctypes.c_char_p
+    if path is None:
+        _lib = lib
+    return lib
+
+
+# Every exported symbol of the C ABI (include/s2tc_gb300.h).
+EXPORTED_SYMBOLS = (
+    "tx_compress_dxtn", "fetch_2d_texel_rgb_dxt1", "fetch_2d_texel_rgba_dxt1",
+    "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5", "rgb565_image",
+    "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
+    "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_last_error",
+)
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    raise TypeError(type(a))
+
+
+def last_error() -> str:
+    return load().s2tc_last_error().decode()
+
+
+def options(dither=DITHER_SIMPLE, metric=WAVG, nrandom=-1, refine=REFINE_ALWAYS) -> Options:
+    return Options(int(dither), int(metric), int(nrandom), int(refine))
+
+
+def options_from_env() -> Options:
+    o = Options()
+    load().s2tc_options_from_env(ctypes.byref(o))
+    return o
+
+
+def set_env(dither=None, metric=None, nrandom=None, refine=None) -> None:
+    """Set the S2TC_* environment knobs that tx_compress_dxtn reads (None
+    removes a knob)."""
+    for key, val, names in (("S2TC_DITHER_MODE", dither, DITHER_NAMES),
+                            ("S2TC_COLORDIST_MODE", metric, COLORDIST_NAMES),
+                            ("S2TC_RANDOM_COLORS", nrandom, None),
+                            ("S2TC_REFINE_COLORS", refine, REFINE_NAMES)):
+        if val is None:
+            os.environ.pop(key, None)
+        elif isinstance(val, str):
+            os.environ[key] = val
+        else:
+            os.environ[key] = str(val) if names is None else names[int(val)]
+
+
+def tx_compress_dxtn(srccomps: int, width: int, height: int, src, destformat: int,
+                     dstRowStride: int = 0, dest: np.ndarray | None = None) -> np.ndarray:
+    """Compress host pixels through the reference-compatible C entry point.
+
+    ``src`` is a packed uint8 array (``width*height*srccomps`` bytes).  Returns
+    the destination buffer (allocated packed unless ``dest`` is given)."""
+    src = np.ascontiguousarray(src, dtype=np.uint8)
+    if dest is None:
+        dest = np.zeros(compressed_size(width, height, destformat) if destformat in FORMATS else 0, np.uint8)
+    load().tx_compress_dxtn(srccomps, width, height, _ptr(src), destformat, _ptr(dest), dstRowStride)
+    return dest
+
+
+def rgb565_image(rgba, w: int, h: int, srccomps: int, alphabits: int, dither: int) -> np.ndarray:
+    rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+    out = np.zeros(w * h * 4, np.uint8)
+    load().rgb565_image(_ptr(out), _ptr(rgba), w, h, srccomps, alphabits, dither)
+    return out
+
+
+_BLOCKFN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                            ctypes.c_int, ctypes.c_int)
+
+
+def encode_block_func(dxt: int, cd: int, nrandom: int, refine: int):
+    """``s2tc_encode_block_func``: returns f(out, rgba565, iw, w, h, nrandom)
+    taking numpy arrays (``rgba565`` may be an offset view of a texel image)."""
+    addr = load().s2tc_encode_block_func(dxt, cd, nrandom, refine)
+    fn = _BLOCKFN(addr)
+
+    def call(out: np.ndarray, rgba: np.ndarray, iw: int, w: int, h: int, nr: int) -> None:
+        fn(_ptr(out), _ptr(rgba), iw, w, h, nr)
+
+    return call
+
+
+def fetch_texel(destformat: int, stride: int, data: np.ndarray, i: int, j: int) -> np.ndarray:
+    lib = load()
+    f = {GL_COMPRESSED_RGB_S3TC_DXT1_EXT: lib.fetch_2d_texel_rgb_dxt1,
+         GL_COMPRESSED_RGBA_S3TC_DXT1_EXT: lib.fetch_2d_texel_rgba_dxt1,
+         GL_COMPRESSED_RGBA_S3TC_DXT3_EXT: lib.fetch_2d_texel_rgba_dxt3,
+         GL_COMPRESSED_RGBA_S3TC_DXT5_EXT: lib.fetch_2d_texel_rgba_dxt5}[destformat]
+    t = np.zeros(4, np.uint8)
+    f(stride, _ptr(data), i, j, _ptr(t))
+    return t
+
+
+def rand_words(width: int, height: int, destformat: int, opt: Options) -> int:
+    return int(load().s2tc_rand_words(width, height, destformat, ctypes.byref(opt)))
+
+
+def gpu_compress(srccomps: int, width: int, height: int, d_src, destformat: int, d_dst,
+                 dst_pitch: int | None = None, opt: Options | None = None, d_rand=None,
+                 stream: int | None = None) -> None:
+    """Compress an image resident in device memory (torch CUDA tensors or raw
+    device pointers) on ``stream`` (a raw cudaStream_t value; None = the
+    library's stream)."""
+    if dst_pitch is None:
+        dst_pitch = ((width + 3) // 4) * block_bytes(destformat)
+    opt = opt if opt is not None else options_from_env()
+    src_p = d_src if isinstance(d_src, int) else _ptr(d_src)
+    dst_p = d_dst if isinstance(d_dst, int) else _ptr(d_dst)
+    rnd_p = None if d_rand is None else (d_rand if isinstance(d_rand, int) else _ptr(d_rand))
+    st = load().s2tc_gpu_compress(srccomps, width, height, src_p, destformat, dst_p, dst_pitch,
+                                  ctypes.byref(opt), rnd_p, stream)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_compress failed ({st}): {last_error()}")
+
+
+def gpu_synchronize(stream: int | None = None) -> None:
+    st = load().s2tc_gpu_synchronize(stream)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_synchronize failed ({st}): {last_error()}")

@@ -1,0 +1,575 @@
+// capi.cpp -- the C ABI of libs2tc_gb300.so: the reference's libtxc_dxtn entry
+// points (tx_compress_dxtn, fetch_2d_texel_*), its encoder API
+// (s2tc_encode_block_func, rgb565_image) and the GPU extension API.
+//
+// The host layer owns one CUDA stream and a grow-only device arena per
+// process; every compression is dither kernel -> block encoder kernel on that
+// stream.  There is no CPU encoding path: when CUDA is unavailable the entry
+// points report the error and write nothing.
+#include "s2tc_gb300.h"
+
+#include <cuda_runtime.h>
+#include <strings.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "dither.h"
+#include "encode.h"
+#include "s2tc_types.h"
+
+namespace s2tc {
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) {
+  g_last_error = msg;
+  std::fprintf(stderr, "s2tc_gb300: %s\n", msg.c_str());
+}
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  bool reserve(size_t n, const char* what) {
+    if (n <= cap) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 4096;
+    if (!cuda_ok(cudaMalloc(&p, want), what)) return false;
+    cap = want;
+    return true;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  bool reserve(size_t n, const char* what) {
+    if (n <= cap) return true;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n + n / 4 + 4096;
+    if (!cuda_ok(cudaMallocHost(&p, want), what)) return false;
+    cap = want;
+    return true;
+  }
+};
+
+// Process-wide GPU context: stream + arena.  Calls are serialised by `mu`.
+struct Context {
+  std::mutex mu;
+  bool ready = false;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t arena_free = nullptr;  // recorded after the last work that used the arena
+  DevBuf src, t565, dst, scratch, rnd, err;
+  PinnedBuf host_rnd, host_out;
+
+  bool init() {
+    if (ready) return true;
+    int n = 0;
+    if (!cuda_ok(cudaGetDeviceCount(&n), "cudaGetDeviceCount")) return false;
+    if (n == 0) {
+      set_error("no CUDA device");
+      return false;
+    }
+    if (!cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate")) return false;
+    if (!cuda_ok(cudaEventCreateWithFlags(&arena_free, cudaEventDisableTiming), "cudaEventCreate")) return false;
+    if (!err.reserve(sizeof(int) * 4, "cudaMalloc(error flag)")) return false;
+    if (!cuda_ok(cudaMemset(err.p, 0, sizeof(int) * 4), "cudaMemset")) return false;
+    ready = true;
+    return true;
+  }
+};
+
+Context& ctx() {
+  static Context* c = new Context();  // never destroyed: CUDA may be torn down first at exit
+  return *c;
+}
+
+int format_dxt(unsigned int fmt) {
+  switch (fmt) {
+    case S2TC_GL_COMPRESSED_RGB_S3TC_DXT1_EXT:
+    case S2TC_GL_COMPRESSED_RGBA_S3TC_DXT1_EXT: return DXT1;
+    case S2TC_GL_COMPRESSED_RGBA_S3TC_DXT3_EXT: return DXT3;
+    case S2TC_GL_COMPRESSED_RGBA_S3TC_DXT5_EXT: return DXT5;
+    default: return -1;
+  }
+}
+
+// Environment knobs, parsed exactly as s2tc_libtxc_dxtn.cpp:156-216.
+s2tc_options read_env() {
+  s2tc_options o;
+  o.metric = CD_WAVG;
+  o.nrandom = -1;
+  o.refine = RF_ALWAYS;
+  o.dither = DI_SIMPLE;
+  if (const char* v = std::getenv("S2TC_DITHER_MODE")) {
+    if (!strcasecmp(v, "NONE")) o.dither = DI_NONE;
+    else if (!strcasecmp(v, "SIMPLE")) o.dither = DI_SIMPLE;
+    else if (!strcasecmp(v, "FLOYDSTEINBERG")) o.dither = DI_FLOYDSTEINBERG;
+    else std::fprintf(stderr, "Invalid dither mode: %s\n", v);
+  }
+  if (const char* v = std::getenv("S2TC_COLORDIST_MODE")) {
+    if (!strcasecmp(v, "RGB")) o.metric = CD_RGB;
+    else if (!strcasecmp(v, "YUV")) o.metric = CD_YUV;
+    else if (!strcasecmp(v, "SRGB")) o.metric = CD_SRGB;
+    else if (!strcasecmp(v, "SRGB_MIXED")) o.metric = CD_SRGB_MIXED;
+    else if (!strcasecmp(v, "AVG")) o.metric = CD_AVG;
+    else if (!strcasecmp(v, "WAVG")) o.metric = CD_WAVG;
+    else if (!strcasecmp(v, "W0AVG")) o.metric = CD_W0AVG;
+    else if (!strcasecmp(v, "NORMALMAP")) o.metric = CD_NORMALMAP;
+    else std::fprintf(stderr, "Invalid color dist mode: %s\n", v);
+  }
+  if (const char* v = std::getenv("S2TC_RANDOM_COLORS")) o.nrandom = std::atoi(v);
+  if (const char* v = std::getenv("S2TC_REFINE_COLORS")) {
+    if (!strcasecmp(v, "NEVER")) o.refine = RF_NEVER;
+    else if (!strcasecmp(v, "ALWAYS")) o.refine = RF_ALWAYS;
+    else if (!strcasecmp(v, "LOOP")) o.refine = RF_LOOP;
+    else std::fprintf(stderr, "Invalid refinement mode: %s\n", v);
+  }
+  return o;
+}
+
+// Out-of-range enum values select the reference's `default:` branches.
+s2tc_options normalise(const s2tc_options& in) {
+  s2tc_options o = in;
+  if (o.dither != DI_NONE && o.dither != DI_FLOYDSTEINBERG) o.dither = DI_SIMPLE;
+  if (o.metric < 0 || o.metric > 7) o.metric = CD_WAVG;
+  if (o.refine != RF_NEVER && o.refine != RF_LOOP) o.refine = RF_ALWAYS;
+  return o;
+}
+
+// The random-candidate search runs when the all-texels mode is selected
+// (nrandom >= 0, or NORMALMAP which never uses the quick mode) and nrandom > 0.
+bool normal_mode(const s2tc_options& o) { return o.nrandom >= 0 || o.metric == CD_NORMALMAP; }
+int rand_per_block(const s2tc_options& o, int dxt) {
+  return (normal_mode(o) && o.nrandom > 0) ? o.nrandom * (dxt == DXT5 ? 4 : 3) : 0;
+}
+
+// Rand words for one chunk of blocks: libc rand(), in the reference's call
+// order, into pinned memory, then to the device.
+constexpr long long kRandChunkWords = 1ll << 24;
+
+int compress_device_locked(Context& c, int srccomps, int width, int height, const uint8_t* d_src, int dxt,
+                           uint8_t* d_dst, long long pitch, const s2tc_options& opt, const unsigned int* d_rand,
+                           cudaStream_t s) {
+  const int sc = srccomps == 3 ? 3 : 4;
+  const long long npx = (long long)width * height;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4;
+  if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return ST_OUT_OF_MEMORY;
+  size_t scratch = dither_scratch_bytes(npx);
+  if (opt.dither == DI_FLOYDSTEINBERG) scratch = dither_fs_scratch_bytes(width, height);
+  if (!c.scratch.reserve(scratch, "cudaMalloc(scratch)")) return ST_OUT_OF_MEMORY;
+  // the arena may still be in use by work on another stream
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return ST_CUDA_ERROR;
+
+  DitherArgs da{};
+  da.src = d_src;
+  da.width = width;
+  da.height = height;
+  da.srccomps = sc;
+  da.alphabits = alpha_bits(dxt);
+  da.dst = c.t565.as<uint32_t>();
+  da.error = c.err.as<int>();
+  if (!cuda_ok(launch_dither(da, opt.dither, c.scratch.as<uint8_t>(), s), "dither launch")) return ST_CUDA_ERROR;
+
+  EncodeArgs ea{};
+  ea.t565 = c.t565.as<uint32_t>();
+  ea.width = width;
+  ea.height = height;
+  ea.bw = bw;
+  ea.bh = bh;
+  ea.dst = d_dst;
+  ea.pitch = pitch;
+  const int bs = block_bytes(dxt);
+  ea.aligned = ((reinterpret_cast<uintptr_t>(d_dst) % bs) == 0 && (pitch % bs) == 0) ? 1 : 0;
+  ea.nrandom = opt.nrandom;
+  ea.prev_a1_first = -1;
+  ea.leftover_out = nullptr;
+  const bool normal = normal_mode(opt);
+  const int per_block = rand_per_block(opt, dxt);
+  if (per_block == 0) {
+    ea.by0 = 0;
+    ea.nby = bh;
+    ea.rnd = nullptr;
+    if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
+  } else {
+    // block rows in chunks so the replayed rand words stay bounded
+    const long long row_words = (long long)bw * per_block;
+    int rows_per_chunk = int(std::max(1ll, kRandChunkWords / std::max(1ll, row_words)));
+    if (!d_rand) {
+      const size_t chunk_bytes = size_t(std::min<long long>(bh, rows_per_chunk)) * row_words * 4;
+      if (!c.rnd.reserve(chunk_bytes, "cudaMalloc(rand)")) return ST_OUT_OF_MEMORY;
+      if (!c.host_rnd.reserve(chunk_bytes, "cudaMallocHost(rand)")) return ST_OUT_OF_MEMORY;
+    }
+    for (int by0 = 0; by0 < bh; by0 += rows_per_chunk) {
+      const int nby = std::min(rows_per_chunk, bh - by0);
+      const long long words = (long long)nby * row_words;
+      ea.by0 = by0;
+      ea.nby = nby;
+      if (d_rand) {
+        ea.rnd = d_rand + (long long)by0 * row_words;
+      } else {
+        // the previous chunk's upload must finish before the staging buffer is refilled
+        if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return ST_CUDA_ERROR;
+        unsigned int* h = static_cast<unsigned int*>(c.host_rnd.p);
+        for (long long i = 0; i < words; ++i) h[i] = unsigned(std::rand());
+        if (!cuda_ok(cudaMemcpyAsync(c.rnd.p, h, size_t(words) * 4, cudaMemcpyHostToDevice, s), "rand upload"))
+          return ST_CUDA_ERROR;
+        ea.rnd = c.rnd.as<uint32_t>();
+      }
+      if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
+    }
+  }
+  if (!cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord")) return ST_CUDA_ERROR;
+  return ST_OK;
+}
+
+// Waits for `s`, then reads and clears the kernels' sticky timeout flag.
+int check_error_flag(Context& c, cudaStream_t s) {
+  int flag = 0;
+  if (!cuda_ok(cudaMemcpyAsync(&flag, c.err.p, sizeof(int), cudaMemcpyDeviceToHost, s), "error flag read"))
+    return ST_CUDA_ERROR;
+  if (!cuda_ok(cudaMemsetAsync(c.err.p, 0, sizeof(int), s), "cudaMemsetAsync")) return ST_CUDA_ERROR;
+  if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return ST_CUDA_ERROR;
+  if (flag) {
+    set_error("a bounded wait in the dither scan gave up");
+    return ST_TIMEOUT;
+  }
+  return ST_OK;
+}
+
+// Host-memory compression used by tx_compress_dxtn.
+void compress_host(int srccomps, int width, int height, const unsigned char* src, int dxt, unsigned char* dest,
+                   int dstRowStride, const s2tc_options& opt) {
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return;
+  cudaStream_t s = c.stream;
+  const int sc = srccomps == 3 ? 3 : 4;
+  const size_t in_bytes = size_t(width) * height * sc;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
+  const size_t row_bytes = size_t(bw) * bs;
+  if (!c.src.reserve(in_bytes + 16, "cudaMalloc(src)")) return;
+  if (!c.dst.reserve(row_bytes * bh + 16, "cudaMalloc(dst)")) return;
+  if (!cuda_ok(cudaMemcpyAsync(c.src.p, src, in_bytes, cudaMemcpyHostToDevice, s), "input upload")) return;
+  if (compress_device_locked(c, sc, width, height, c.src.as<uint8_t>(), dxt, c.dst.as<uint8_t>(), (long long)row_bytes,
+                             opt, nullptr, s) != ST_OK)
+    return;
+  if (check_error_flag(c, s) != ST_OK) return;
+  // Output rows: packed, or dstRowStride apart (s2tc_libtxc_dxtn.cpp:243, 261, 279).
+  const long long diff =
+      dstRowStride >= width * (bs / 4) ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs / 4) : 0;
+  if (diff == 0) {
+    cuda_ok(cudaMemcpyAsync(dest, c.dst.p, row_bytes * bh, cudaMemcpyDeviceToHost, s), "output download");
+  } else if (diff > 0) {
+    cuda_ok(cudaMemcpy2DAsync(dest, row_bytes + diff, c.dst.p, row_bytes, row_bytes, bh, cudaMemcpyDeviceToHost, s),
+            "output download");
+  } else {
+    // overlapping rows: later rows overwrite the end of earlier ones, in order
+    if (!c.host_out.reserve(row_bytes * bh, "cudaMallocHost(output)")) return;
+    if (!cuda_ok(cudaMemcpyAsync(c.host_out.p, c.dst.p, row_bytes * bh, cudaMemcpyDeviceToHost, s), "output download"))
+      return;
+    if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return;
+    for (int r = 0; r < bh; ++r)
+      std::memmove(dest + r * (long long)(row_bytes + diff), static_cast<unsigned char*>(c.host_out.p) + r * row_bytes,
+                   row_bytes);
+    return;
+  }
+  cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
+// ----------------------------------------------------------- block shims
+
+// Leftover second alpha endpoint of the previous shim call on this thread,
+// read by a following single-texel DXT5 block (see encode.cu).
+thread_local int g_prev_a1 = -1;
+
+void encode_one_block(int dxt, int metric, bool normal, int refine, unsigned char* out, const unsigned char* rgba,
+                      int iw, int w, int h, int nrandom) {
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return;
+  cudaStream_t s = c.stream;
+  if (w < 1 || h < 1) return;
+  w = w > 4 ? 4 : w;
+  h = h > 4 ? 4 : h;
+  // gather the block's rows into a packed w x h texel image
+  uint32_t blk[16] = {0};
+  for (int y = 0; y < h; ++y) std::memcpy(&blk[y * w], rgba + (size_t)y * iw * 4, size_t(w) * 4);
+  s2tc_options opt{DI_NONE, metric, nrandom, refine};
+  const int per_block = (normal && nrandom > 0) ? nrandom * (dxt == DXT5 ? 4 : 3) : 0;
+  if (!c.t565.reserve(64 + 16, "cudaMalloc(texels)")) return;
+  if (!c.dst.reserve(16, "cudaMalloc(dst)")) return;
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return;
+  if (per_block > 0) {
+    if (!c.rnd.reserve(size_t(per_block) * 4, "cudaMalloc(rand)")) return;
+    if (!c.host_rnd.reserve(size_t(per_block) * 4, "cudaMallocHost(rand)")) return;
+    unsigned int* hr = static_cast<unsigned int*>(c.host_rnd.p);
+    for (int i = 0; i < per_block; ++i) hr[i] = unsigned(std::rand());
+    if (!cuda_ok(cudaMemcpyAsync(c.rnd.p, hr, size_t(per_block) * 4, cudaMemcpyHostToDevice, s), "rand upload")) return;
+  }
+  if (!cuda_ok(cudaMemcpyAsync(c.t565.p, blk, sizeof(blk), cudaMemcpyHostToDevice, s), "block upload")) return;
+  EncodeArgs ea{};
+  ea.t565 = c.t565.as<uint32_t>();
+  ea.width = w;
+  ea.height = h;
+  ea.bw = 1;
+  ea.bh = 1;
+  ea.by0 = 0;
+  ea.nby = 1;
+  ea.dst = c.dst.as<uint8_t>();
+  ea.pitch = 16;
+  ea.aligned = 1;
+  ea.nrandom = opt.nrandom;
+  ea.rnd = per_block > 0 ? c.rnd.as<uint32_t>() : nullptr;
+  ea.prev_a1_first = g_prev_a1;
+  ea.leftover_out = c.err.as<int>() + 1;
+  if (!cuda_ok(launch_encode(ea, dxt, metric, normal, refine, s), "encode launch")) return;
+  unsigned char tmp[16];
+  int leftover = -1;
+  if (!cuda_ok(cudaMemcpyAsync(tmp, c.dst.p, 16, cudaMemcpyDeviceToHost, s), "block download")) return;
+  if (!cuda_ok(cudaMemcpyAsync(&leftover, c.err.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, s),
+               "block download"))
+    return;
+  if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return;
+  std::memcpy(out, tmp, size_t(block_bytes(dxt)));
+  g_prev_a1 = leftover;
+}
+
+template <int DXT, int METRIC, bool NORMAL, int REFINE>
+void block_shim(unsigned char* out, const unsigned char* rgba, int iw, int w, int h, int nrandom) {
+  encode_one_block(DXT, METRIC, NORMAL, REFINE, out, rgba, iw, w, h, nrandom);
+}
+
+template <int DXT, int METRIC, bool NORMAL>
+s2tc_encode_block_func_t pick_refine(int refine) {
+  switch (refine) {
+    case RF_NEVER: return &block_shim<DXT, METRIC, NORMAL, RF_NEVER>;
+    case RF_LOOP: return &block_shim<DXT, METRIC, NORMAL, RF_LOOP>;
+    default: return &block_shim<DXT, METRIC, NORMAL, RF_ALWAYS>;
+  }
+}
+template <int DXT, int METRIC>
+s2tc_encode_block_func_t pick_mode(int nrandom, int refine) {
+  if (METRIC == CD_NORMALMAP || nrandom >= 0) return pick_refine<DXT, METRIC, true>(refine);
+  return pick_refine<DXT, METRIC, false>(refine);
+}
+template <int METRIC>
+s2tc_encode_block_func_t pick_dxt(int dxt, int nrandom, int refine) {
+  switch (dxt) {
+    case DXT1: return pick_mode<DXT1, METRIC>(nrandom, refine);
+    case DXT3: return pick_mode<DXT3, METRIC>(nrandom, refine);
+    default: return pick_mode<DXT5, METRIC>(nrandom, refine);
+  }
+}
+
+// ---------------------------------------------------------- texel decode
+
+void expand565(unsigned c, unsigned char* t) {
+  const int r = (c >> 11) & 31, g = (c >> 5) & 63, b = c & 31;
+  t[0] = (unsigned char)((r << 3) | (r >> 2));
+  t[1] = (unsigned char)((g << 2) | (g >> 4));
+  t[2] = (unsigned char)((b << 3) | (b >> 2));
+}
+
+// s2tc_libtxc_dxtn.cpp:35-140: decode texel (i, j).
+void fetch_texel(int dxt, bool rgba_dxt1, int stride, const unsigned char* data, int i, int j, unsigned char* t) {
+  const int bs = dxt == DXT1 ? 8 : 16;
+  const unsigned char* blk = data + ((long long)((stride + 3) >> 2) * (j >> 2) + (i >> 2)) * bs;
+  const unsigned char* cb = blk + (bs - 8);
+  unsigned c = cb[0] | (cb[1] << 8), c1 = cb[2] | (cb[3] << 8);
+  const int sel = (cb[4 + (j & 3)] >> (2 * (i & 3))) & 3;
+  const bool odd = ((i ^ j) & 1) != 0;
+  unsigned char a = 255;
+  if (sel == 1) {
+    c = c1;
+  } else if (sel >= 2) {
+    if (dxt == DXT1 && sel == 3 && c1 >= c) {
+      c = 0;
+      if (rgba_dxt1) a = 0;
+    } else if (odd) {
+      c = c1;
+    }
+  }
+  expand565(c, t);
+  if (dxt == DXT1) {
+    if (rgba_dxt1) t[3] = a;
+    return;
+  }
+  if (dxt == DXT3) {
+    const int av = (blk[(j & 3) * 2 + ((i & 3) >> 1)] >> (4 * (i & 1))) & 15;
+    t[3] = (unsigned char)(av | (av << 4));
+    return;
+  }
+  unsigned a0 = blk[0], a1 = blk[1];
+  const int bit = ((j & 3) * 4 + (i & 3)) * 3;
+  int ab = 0;
+  for (int k = 0; k < 3; ++k)
+    if (blk[2 + ((bit + k) >> 3)] & (1 << ((bit + k) & 7))) ab |= 1 << k;
+  unsigned av = a0;
+  if (ab == 1) av = a1;
+  else if (ab == 6 && a1 >= a0) av = 0;
+  else if ((ab == 6 || ab == 7) && a1 >= a0) av = 255;
+  else if (ab >= 2 && odd) av = a1;
+  t[3] = (unsigned char)av;
+}
+
+}  // namespace
+}  // namespace s2tc
+
+using s2tc::Context;
+using s2tc::DitherArgs;
+using s2tc::check_error_flag;
+using s2tc::compress_device_locked;
+using s2tc::compress_host;
+using s2tc::ctx;
+using s2tc::cuda_ok;
+using s2tc::fetch_texel;
+using s2tc::format_dxt;
+using s2tc::normalise;
+using s2tc::pick_dxt;
+using s2tc::rand_per_block;
+using s2tc::read_env;
+using s2tc::set_error;
+
+extern "C" {
+
+void tx_compress_dxtn(int srccomps, int width, int height, const unsigned char* srcPixData, unsigned int destformat,
+                      unsigned char* dest, int dstRowStride) {
+  const s2tc_options opt = read_env();
+  const int dxt = format_dxt(destformat);
+  if (dxt < 0) {
+    std::fprintf(stderr, "libdxtn: Bad dstFormat %d in tx_compress_dxtn\n", (int)destformat);
+    return;
+  }
+  if (width <= 0 || height <= 0) return;
+  compress_host(srccomps, width, height, srcPixData, dxt, dest, dstRowStride, normalise(opt));
+}
+
+void fetch_2d_texel_rgb_dxt1(int srcRowStride, const unsigned char* pixdata, int i, int j, void* texel) {
+  unsigned char* t = static_cast<unsigned char*>(texel);
+  fetch_texel(s2tc::DXT1, false, srcRowStride, pixdata, i, j, t);
+  t[3] = 255;
+}
+void fetch_2d_texel_rgba_dxt1(int srcRowStride, const unsigned char* pixdata, int i, int j, void* texel) {
+  fetch_texel(s2tc::DXT1, true, srcRowStride, pixdata, i, j, static_cast<unsigned char*>(texel));
+}
+void fetch_2d_texel_rgba_dxt3(int srcRowStride, const unsigned char* pixdata, int i, int j, void* texel) {
+  fetch_texel(s2tc::DXT3, true, srcRowStride, pixdata, i, j, static_cast<unsigned char*>(texel));
+}
+void fetch_2d_texel_rgba_dxt5(int srcRowStride, const unsigned char* pixdata, int i, int j, void* texel) {
+  fetch_texel(s2tc::DXT5, true, srcRowStride, pixdata, i, j, static_cast<unsigned char*>(texel));
+}
+
+void rgb565_image(unsigned char* out, const unsigned char* rgba, int w, int h, int srccomps, int alphabits,
+                  DitherMode dither) {
+  if (w <= 0 || h <= 0) return;
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return;
+  cudaStream_t s = c.stream;
+  const int sc = srccomps == 3 ? 3 : 4;
+  const int ab = alphabits == 1 ? 1 : alphabits == 4 ? 4 : 8;
+  int d = int(dither);
+  if (d != s2tc::DI_NONE && d != s2tc::DI_FLOYDSTEINBERG) d = s2tc::DI_SIMPLE;
+  const long long npx = (long long)w * h;
+  if (!c.src.reserve(size_t(npx) * sc + 16, "cudaMalloc(src)")) return;
+  if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return;
+  size_t scratch = d == s2tc::DI_FLOYDSTEINBERG ? s2tc::dither_fs_scratch_bytes(w, h) : s2tc::dither_scratch_bytes(npx);
+  if (!c.scratch.reserve(scratch, "cudaMalloc(scratch)")) return;
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return;
+  if (!cuda_ok(cudaMemcpyAsync(c.src.p, rgba, size_t(npx) * sc, cudaMemcpyHostToDevice, s), "input upload")) return;
+  DitherArgs da{};
+  da.src = c.src.as<uint8_t>();
+  da.width = w;
+  da.height = h;
+  da.srccomps = sc;
+  da.alphabits = ab;
+  da.dst = c.t565.as<uint32_t>();
+  da.error = c.err.as<int>();
+  if (!cuda_ok(s2tc::launch_dither(da, d, c.scratch.as<uint8_t>(), s), "dither launch")) return;
+  if (check_error_flag(c, s) != s2tc::ST_OK) return;
+  if (!cuda_ok(cudaMemcpyAsync(out, c.t565.p, size_t(npx) * 4, cudaMemcpyDeviceToHost, s), "output download")) return;
+  cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
+s2tc_encode_block_func_t s2tc_encode_block_func(DxtMode dxt, ColorDistMode cd, int nrandom, RefinementMode refine) {
+  const int d = int(dxt), r = int(refine);
+  switch (int(cd)) {
+    case s2tc::CD_RGB: return pick_dxt<s2tc::CD_RGB>(d, nrandom, r);
+    case s2tc::CD_YUV: return pick_dxt<s2tc::CD_YUV>(d, nrandom, r);
+    case s2tc::CD_SRGB: return pick_dxt<s2tc::CD_SRGB>(d, nrandom, r);
+    case s2tc::CD_SRGB_MIXED: return pick_dxt<s2tc::CD_SRGB_MIXED>(d, nrandom, r);
+    case s2tc::CD_AVG: return pick_dxt<s2tc::CD_AVG>(d, nrandom, r);
+    case s2tc::CD_W0AVG: return pick_dxt<s2tc::CD_W0AVG>(d, nrandom, r);
+    case s2tc::CD_NORMALMAP: return pick_dxt<s2tc::CD_NORMALMAP>(d, nrandom, r);
+    default: return pick_dxt<s2tc::CD_WAVG>(d, nrandom, r);
+  }
+}
+
+void s2tc_options_from_env(s2tc_options* opt) {
+  if (opt) *opt = read_env();
+}
+
+long long s2tc_rand_words(int width, int height, unsigned int destformat, const s2tc_options* opt) {
+  const int dxt = format_dxt(destformat);
+  if (dxt < 0 || !opt || width <= 0 || height <= 0) return 0;
+  const s2tc_options o = normalise(*opt);
+  return (long long)((width + 3) / 4) * ((height + 3) / 4) * rand_per_block(o, dxt);
+}
+
+int s2tc_gpu_compress(int srccomps, int width, int height, const void* d_src, unsigned int destformat, void* d_dst,
+                      long long dst_pitch, const s2tc_options* opt, const unsigned int* d_rand, void* stream) {
+  const int dxt = format_dxt(destformat);
+  if (dxt < 0) {
+    set_error("bad destination format");
+    return S2TC_ERR_FORMAT;
+  }
+  if (width < 0 || height < 0 || !opt || (width > 0 && height > 0 && (!d_src || !d_dst))) {
+    set_error("bad argument");
+    return S2TC_ERR_ARGUMENT;
+  }
+  if (width == 0 || height == 0) return S2TC_OK;
+  const int bw = (width + 3) / 4;
+  if (dst_pitch < (long long)bw * s2tc::block_bytes(dxt)) {
+    set_error("dst_pitch smaller than a block row");
+    return S2TC_ERR_ARGUMENT;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+  return compress_device_locked(c, srccomps, width, height, static_cast<const uint8_t*>(d_src), dxt,
+                                static_cast<uint8_t*>(d_dst), dst_pitch, normalise(*opt), d_rand, s);
+}
+
+int s2tc_gpu_synchronize(void* stream) {
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  return check_error_flag(c, stream ? static_cast<cudaStream_t>(stream) : c.stream);
+}
+
+const char* s2tc_last_error(void) { return s2tc::g_last_error.c_str(); }
+
+}  // extern "C"

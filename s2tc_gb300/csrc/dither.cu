@@ -1,0 +1,353 @@
+// dither.cu -- RGB8/RGBA8 -> 5:6:5 texel words with the reference's dither
+// modes (s2tc_algorithm.cpp:1196-1465).
+//
+// DITHER_NONE is elementwise.  DITHER_SIMPLE is one serial error-diffusion
+// chain per channel over the whole image in raster order; it is computed here
+// as an exact single-pass scan:
+//   - a channel's carried error takes few values (red/blue: -7..7, green:
+//     -3..3, 4-bit alpha: -15..15), so the effect of a run of texels on it is a
+//     small table state -> state; tables compose;
+//   - each thread builds the table of its 16-texel segment, the CTA composes
+//     them (Hillis-Steele in shared memory), tiles chain their aggregates with
+//     a decoupled look-back, and every thread then replays its segment from
+//     its exact start state;
+//   - the 1-bit alpha chain (diffuse1) is a rotation: its carried error after
+//     k texels is ((sum of sources + 127) mod 255) - 127, so its "table" is a
+//     sum mod 255.
+// The look-back spins are bounded; on timeout the kernel records an error
+// flag and finishes, and the host reports it.
+#include <cuda/atomic>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "dither.h"
+
+namespace s2tc {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kSeg = 16;
+constexpr int kTile = kThreads * kSeg;
+
+// Table layout (bytes) inside one 72-byte record: red 15 states at 0, green 7
+// at 16, blue 15 at 24, alpha at 40 (31 states for 4-bit, or one byte holding
+// the mod-255 sum for 1-bit).
+constexpr int kOffR = 0, kOffG = 16, kOffB = 24, kOffA = 40;
+constexpr int kRec = 72;
+
+// One step of the 1-D error diffusion (s2tc_algorithm.cpp:1198-1207).
+template <int SHIFT>
+__device__ __forceinline__ int qstep(int& d, int src) {
+  constexpr int maxv = (1 << (8 - SHIFT)) - 1;
+  const int v = src + d;
+  const int q = min(max(v >> SHIFT, 0), maxv);
+  d = v - ((q << SHIFT) | (q >> (8 - 2 * SHIFT)));
+  return q;
+}
+
+template <int SHIFT>
+struct QChan {
+  static constexpr int kOff = (1 << SHIFT) - 1;  // largest carried error
+  static constexpr int kStates = 2 * kOff + 1;
+};
+
+__device__ __forceinline__ int chan_of(uint32_t px, int c) { return int((px >> (8 * c)) & 0xFF); }
+
+// Table of one channel over the thread's segment: entry s is the end state
+// when the segment starts in state s.
+template <int SHIFT>
+__device__ __forceinline__ void seg_table(const uint32_t* px, int nvalid, int c, uint8_t* out) {
+  using Q = QChan<SHIFT>;
+#pragma unroll 1
+  for (int s = 0; s < Q::kStates; ++s) {
+    int d = s - Q::kOff;
+#pragma unroll
+    for (int k = 0; k < kSeg; ++k)
+      if (k < nvalid) qstep<SHIFT>(d, chan_of(px[k], c));
+    out[s] = uint8_t(d + Q::kOff);
+  }
+}
+
+// dst = apply `first`, then `second`.
+template <int AK>
+__device__ __forceinline__ void compose(const uint8_t* first, const uint8_t* second, uint8_t* dst) {
+#pragma unroll 1
+  for (int s = 0; s < QChan<3>::kStates; ++s) {
+    dst[kOffR + s] = second[kOffR + first[kOffR + s]];
+    dst[kOffB + s] = second[kOffB + first[kOffB + s]];
+  }
+#pragma unroll 1
+  for (int s = 0; s < QChan<2>::kStates; ++s) dst[kOffG + s] = second[kOffG + first[kOffG + s]];
+  if (AK == 4) {
+#pragma unroll 1
+    for (int s = 0; s < QChan<4>::kStates; ++s) dst[kOffA + s] = second[kOffA + first[kOffA + s]];
+  } else if (AK == 1) {
+    dst[kOffA] = uint8_t((first[kOffA] + second[kOffA]) % 255);
+  }
+}
+
+// Apply a table record to packed start states (r | g<<8 | b<<16 | a<<24).
+template <int AK>
+__device__ __forceinline__ uint32_t apply(const uint8_t* t, uint32_t st) {
+  uint32_t r = t[kOffR + (st & 0xFF)];
+  uint32_t g = t[kOffG + ((st >> 8) & 0xFF)];
+  uint32_t b = t[kOffB + ((st >> 16) & 0xFF)];
+  uint32_t a = 0;
+  if (AK == 4) a = t[kOffA + (st >> 24)];
+  if (AK == 1) a = ((st >> 24) + t[kOffA]) % 255;
+  return r | (g << 8) | (b << 16) | (a << 24);
+}
+
+template <int AK>
+__device__ __forceinline__ uint32_t initial_state() {
+  // zero carried error in every chain
+  return uint32_t(QChan<3>::kOff) | (uint32_t(QChan<2>::kOff) << 8) | (uint32_t(QChan<3>::kOff) << 16) |
+         (uint32_t(AK == 4 ? QChan<4>::kOff : AK == 1 ? 127 : 0) << 24);
+}
+
+template <int AK>
+__device__ __forceinline__ void identity(uint8_t* t) {
+  for (int s = 0; s < QChan<3>::kStates; ++s) t[kOffR + s] = t[kOffB + s] = uint8_t(s);
+  for (int s = 0; s < QChan<2>::kStates; ++s) t[kOffG + s] = uint8_t(s);
+  if (AK == 4)
+    for (int s = 0; s < QChan<4>::kStates; ++s) t[kOffA + s] = uint8_t(s);
+  if (AK == 1) t[kOffA] = 0;
+}
+
+// Load the thread's segment (texels [p0, p0 + nvalid)) as RGBA words; for
+// 3-component input the alpha byte is left 0.
+template <int SC>
+__device__ __forceinline__ void load_seg(const uint8_t* __restrict__ src, long long p0, int nvalid, uint32_t* px) {
+  const uint8_t* s = src + p0 * SC;
+  const bool vec = nvalid == kSeg && (reinterpret_cast<uintptr_t>(s) & 15) == 0;
+  if (SC == 4) {
+    if (vec) {
+      const uint4* v = reinterpret_cast<const uint4*>(s);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        uint4 w = __ldg(v + q);
+        px[4 * q + 0] = w.x; px[4 * q + 1] = w.y; px[4 * q + 2] = w.z; px[4 * q + 3] = w.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kSeg; ++k)
+        px[k] = k < nvalid ? (uint32_t(s[4 * k]) | (uint32_t(s[4 * k + 1]) << 8) | (uint32_t(s[4 * k + 2]) << 16) |
+                              (uint32_t(s[4 * k + 3]) << 24))
+                           : 0u;
+    }
+  } else {
+    if (vec) {
+      uint32_t w[12];
+      const uint4* v = reinterpret_cast<const uint4*>(s);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        uint4 t = __ldg(v + q);
+        w[4 * q + 0] = t.x; w[4 * q + 1] = t.y; w[4 * q + 2] = t.z; w[4 * q + 3] = t.w;
+      }
+#pragma unroll
+      for (int k = 0; k < kSeg; ++k) {
+        // texel k occupies bytes 3k..3k+2 of the 48-byte segment
+        const int b0 = 3 * k;
+        uint64_t pair = uint64_t(w[b0 >> 2]) | (uint64_t(w[min((b0 >> 2) + 1, 11)]) << 32);
+        px[k] = uint32_t(pair >> (8 * (b0 & 3))) & 0xFFFFFFu;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kSeg; ++k)
+        px[k] = k < nvalid ? (uint32_t(s[3 * k]) | (uint32_t(s[3 * k + 1]) << 8) | (uint32_t(s[3 * k + 2]) << 16))
+                           : 0u;
+    }
+  }
+}
+
+using Status = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
+constexpr unsigned long long kAggReady = 1ull << 32;
+constexpr unsigned long long kIncReady = 2ull << 32;
+constexpr int kSpinLimit = 1 << 22;
+
+template <int SC, int AK>
+__global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
+  __shared__ __align__(16) uint8_t tbl[2][kThreads][kRec];
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_carry;
+
+  const int t = threadIdx.x;
+  if (t == 0) s_tile = atomicAdd(a.ticket, 1u);
+  __syncthreads();
+  const long long tile = s_tile;
+  const long long npx = (long long)a.width * a.height;
+  const long long p0 = tile * kTile + (long long)t * kSeg;
+  const int nvalid = int(max(0ll, min((long long)kSeg, npx - p0)));
+
+  uint32_t px[kSeg];
+  load_seg<SC>(a.src, p0, nvalid, px);
+
+  // segment tables
+  uint8_t* mine = tbl[0][t];
+  seg_table<3>(px, nvalid, 0, mine + kOffR);
+  seg_table<2>(px, nvalid, 1, mine + kOffG);
+  seg_table<3>(px, nvalid, 2, mine + kOffB);
+  if (AK == 4) seg_table<4>(px, nvalid, 3, mine + kOffA);
+  if (AK == 1) {
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kSeg; ++k)
+      if (k < nvalid) sum += chan_of(px[k], 3);
+    mine[kOffA] = uint8_t(sum % 255);
+  }
+  __syncthreads();
+
+  // inclusive scan of the tables across the CTA
+  int cur = 0;
+  for (int off = 1; off < kThreads; off <<= 1) {
+    if (t >= off) compose<AK>(tbl[cur][t - off], tbl[cur][t], tbl[cur ^ 1][t]);
+    else
+      for (int i = 0; i < kRec; ++i) tbl[cur ^ 1][t][i] = tbl[cur][t][i];
+    __syncthreads();
+    cur ^= 1;
+  }
+
+  // chain the tiles: publish, look back, publish the inclusive state
+  if (t == 0) {
+    const uint8_t* agg = tbl[cur][kThreads - 1];
+    Status st(a.status[tile]);
+    uint32_t carry = initial_state<AK>();
+    if (tile == 0) {
+      st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+    } else {
+      uint8_t* gagg = a.aggs + tile * kRec;
+      for (int i = 0; i < kRec; ++i) gagg[i] = agg[i];
+      st.store(kAggReady, cuda::memory_order_release);
+      // acc: state at the end of tile k -> state at the start of this tile
+      uint8_t acc[kRec];
+      identity<AK>(acc);
+      long long k = tile - 1;
+      for (;;) {
+        Status sk(a.status[k]);
+        unsigned long long v = sk.load(cuda::memory_order_acquire);
+        int spins = 0;
+        while ((v >> 32) == 0 && spins < kSpinLimit) {
+          __nanosleep(64);
+          v = sk.load(cuda::memory_order_acquire);
+          ++spins;
+        }
+        if ((v >> 32) == 0) {
+          atomicExch(a.error, 1);
+          break;
+        }
+        if ((v >> 32) == 2) {
+          carry = apply<AK>(acc, uint32_t(v));
+          break;
+        }
+        // acc := agg[k] then acc
+        uint8_t tmp[kRec];
+        compose<AK>(a.aggs + k * kRec, acc, tmp);
+        for (int i = 0; i < kRec; ++i) acc[i] = tmp[i];
+        --k;
+      }
+      st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+    }
+    s_carry = carry;
+  }
+  __syncthreads();
+
+  // replay the segment from its exact start state
+  uint32_t start = t == 0 ? s_carry : apply<AK>(tbl[cur][t - 1], s_carry);
+  int dr = int(start & 0xFF) - QChan<3>::kOff;
+  int dg = int((start >> 8) & 0xFF) - QChan<2>::kOff;
+  int db = int((start >> 16) & 0xFF) - QChan<3>::kOff;
+  int da = AK == 4 ? int(start >> 24) - QChan<4>::kOff : int(start >> 24) - 127;
+  uint32_t out[kSeg];
+#pragma unroll
+  for (int k = 0; k < kSeg; ++k) {
+    const uint32_t p = px[k];
+    uint32_t q = uint32_t(qstep<3>(dr, chan_of(p, 0))) | (uint32_t(qstep<2>(dg, chan_of(p, 1))) << 8) |
+                 (uint32_t(qstep<3>(db, chan_of(p, 2))) << 16);
+    uint32_t qa;
+    if (AK == 4) {
+      qa = uint32_t(qstep<4>(da, chan_of(p, 3)));
+    } else if (AK == 1) {
+      // diffuse1 (s2tc_algorithm.cpp:1208-1216)
+      const int v = chan_of(p, 3) + da;
+      qa = v >= 128;
+      da = v - (qa ? 255 : 0);
+    } else if (AK == 8) {
+      qa = uint32_t(chan_of(p, 3));
+    } else {
+      qa = uint32_t(a.alpha_const);
+    }
+    out[k] = q | (qa << 24);
+  }
+  uint32_t* o = a.dst + p0;
+  if (nvalid == kSeg) {
+    uint4* v = reinterpret_cast<uint4*>(o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = make_uint4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+  } else {
+    for (int k = 0; k < nvalid; ++k) o[k] = out[k];
+  }
+}
+
+// DITHER_NONE (s2tc_algorithm.cpp:1269-1305): plain truncation.
+template <int SC>
+__global__ void __launch_bounds__(256) k_dither_none(DitherArgs a) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long npx = (long long)a.width * a.height;
+  if (p >= npx) return;
+  const uint8_t* s = a.src + p * SC;
+  uint32_t r = s[0] >> 3, g = s[1] >> 2, b = s[2] >> 3;
+  uint32_t al = SC == 4 ? uint32_t(s[3] >> (8 - a.alphabits)) : uint32_t(a.alpha_const);
+  a.dst[p] = r | (g << 8) | (b << 16) | (al << 24);
+}
+
+template <int SC>
+cudaError_t launch_simple(const DitherArgs& a, cudaStream_t s) {
+  const long long npx = (long long)a.width * a.height;
+  const unsigned grid = unsigned((npx + kTile - 1) / kTile);
+  if (SC == 3) {
+    k_dither_simple<SC, 0><<<grid, kThreads, 0, s>>>(a);
+  } else if (a.alphabits == 1) {
+    k_dither_simple<SC, 1><<<grid, kThreads, 0, s>>>(a);
+  } else if (a.alphabits == 4) {
+    k_dither_simple<SC, 4><<<grid, kThreads, 0, s>>>(a);
+  } else {
+    k_dither_simple<SC, 8><<<grid, kThreads, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t dither_scratch_bytes(long long npx) {
+  const long long tiles = (npx + kTile - 1) / kTile;
+  // status words, aggregate tables, ticket + error flag
+  return size_t(tiles) * (sizeof(unsigned long long) + kRec) + 256;
+}
+
+cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream_t s) {
+  const long long npx = (long long)a.width * a.height;
+  if (npx <= 0) return cudaSuccess;
+  a.alpha_const = (1 << a.alphabits) - 1;
+  if (dither == DI_FLOYDSTEINBERG) return launch_dither_fs(a, scratch, s);
+  if (dither == DI_NONE) {
+    const unsigned grid = unsigned((npx + 255) / 256);
+    if (a.srccomps == 3) k_dither_none<3><<<grid, 256, 0, s>>>(a);
+    else k_dither_none<4><<<grid, 256, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  // DI_SIMPLE (DI_FLOYDSTEINBERG is handled by dither_fs.cu)
+  const long long tiles = (npx + kTile - 1) / kTile;
+  a.status = reinterpret_cast<unsigned long long*>(scratch);
+  a.aggs = scratch + tiles * sizeof(unsigned long long);
+  a.ticket = reinterpret_cast<unsigned int*>(a.aggs + tiles * kRec);
+  a.ticket = reinterpret_cast<unsigned int*>((reinterpret_cast<uintptr_t>(a.ticket) + 15) & ~uintptr_t(15));
+  cudaError_t e = cudaMemsetAsync(a.status, 0, tiles * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  if (a.srccomps == 3) return launch_simple<3>(a, s);
+  return launch_simple<4>(a, s);
+}
+
+}  // namespace s2tc

@@ -1,0 +1,345 @@
+// encode.cu -- the S2TC block encoder kernels (one thread per 4x4 block).
+//
+// This file is compiled once per colour-distance metric (-DS2TC_METRIC=<id>),
+// so the 135 (format x metric x selection x refinement) instantiations of the
+// reference's compile-time dispatch (s2tc_algorithm.cpp:1110-1194) spread over
+// eight translation units that build in parallel.
+//
+// Input: the 4-byte-per-texel 5:6:5 buffer produced by the dither kernels
+// (r | g<<8 | b<<16 | a<<24, row length `width` texels).  Output: 8/16-byte
+// DXT1/DXT3/DXT5 blocks, block rows `pitch` bytes apart.
+#include <cuda_runtime.h>
+
+#include "encode.h"
+#include "s2tc_device.cuh"
+
+#ifndef S2TC_METRIC
+#error "compile with -DS2TC_METRIC=<0..7>"
+#endif
+
+namespace s2tc {
+namespace {
+
+constexpr int kMetric = S2TC_METRIC;
+
+// Candidate c[j] of the pair search: the first n are the block's inputs in
+// x-outer, y-inner order; the rest are the random candidates of
+// s2tc_algorithm.cpp:962-993 drawn from the replayed rand() words.
+struct Candidates {
+  C3 in[16];
+  int ain[16];
+  int n;
+  // random candidates
+  int nr;
+  const uint32_t* rnd;
+  int stride;  // rand words per candidate: 3 (DXT1/DXT3) or 4 (DXT5)
+  C3 lo;
+  int lr, lg, lb;
+  int alo, la;
+};
+
+__device__ __forceinline__ C3 cand_rgb(const Candidates& cs, int j) {
+  if (j < cs.n) return cs.in[j];
+  const uint32_t* r = cs.rnd + size_t(j - cs.n) * cs.stride;
+  return C3{cs.lo.r + int(__ldg(r) % uint32_t(cs.lr)), cs.lo.g + int(__ldg(r + 1) % uint32_t(cs.lg)),
+            cs.lo.b + int(__ldg(r + 2) % uint32_t(cs.lb))};
+}
+__device__ __forceinline__ int cand_a(const Candidates& cs, int j) {
+  if (j < cs.n) return cs.ain[j];
+  const uint32_t* r = cs.rnd + size_t(j - cs.n) * cs.stride;
+  return cs.alo + int(__ldg(r + 3) % uint32_t(cs.la));
+}
+
+// Distance of candidate row i to input k, with the reference's argument order:
+// between two inputs it is dist(c[min], c[max]) (s2tc_algorithm.cpp:375-383),
+// for a random candidate dist(c[i], c[k]) (:385-392).
+__device__ __forceinline__ int32_t in_dist(const Candidates& cs, int i, int k) {
+  if (i == k) return 0;
+  return i < k ? cdist<kMetric>(cs.in[i], cs.in[k]) : cdist<kMetric>(cs.in[k], cs.in[i]);
+}
+
+// reduce_colors_inplace (s2tc_algorithm.cpp:363-414): first pair (i<j) in
+// lexicographic order that the reference's `bestsum < 0 || sum < bestsum`
+// rule keeps.  Sequential over pairs, so the rule is followed literally.
+__device__ void reduce_rgb(const Candidates& cs, int m, C3& c0, C3& c1) {
+  const int n = cs.n;
+  int32_t dm[16][16];
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < n; ++k) dm[i][k] = in_dist(cs, i, k);
+  int32_t bestsum = -1;
+  int besti = 0, bestj = 1;
+  int32_t ri[16], rj[16];
+  for (int i = 0; i < m; ++i) {
+    if (i < n) {
+      for (int k = 0; k < 16; ++k) ri[k] = k < n ? dm[i][k] : 0;
+    } else {
+      C3 ci = cand_rgb(cs, i);
+      for (int k = 0; k < 16; ++k) ri[k] = k < n ? cdist<kMetric>(ci, cs.in[k]) : 0;
+    }
+    for (int j = i + 1; j < m; ++j) {
+      if (j < n) {
+        for (int k = 0; k < 16; ++k) rj[k] = k < n ? dm[j][k] : 0;
+      } else {
+        C3 cj = cand_rgb(cs, j);
+        for (int k = 0; k < 16; ++k) rj[k] = k < n ? cdist<kMetric>(cj, cs.in[k]) : 0;
+      }
+      int32_t sum = 0;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) sum = wadd(sum, min(ri[k], rj[k]));
+      if (bestsum < 0 || sum < bestsum) {
+        bestsum = sum;
+        besti = i;
+        bestj = j;
+      }
+    }
+  }
+  c0 = cand_rgb(cs, besti);
+  c1 = cand_rgb(cs, bestj);
+}
+
+// reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) on the alpha
+// candidates.  Its conditional writes back into c[0]/c[1] read the candidates
+// before any of them changes, so the result is simply the winning pair.
+__device__ void reduce_alpha(const Candidates& cs, int m, int& a0, int& a1) {
+  const int n = cs.n;
+  int32_t fix[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    int a = k < n ? cs.ain[k] : 0;
+    fix[k] = k < n ? min(a * a, (255 - a) * (255 - a)) : 0;
+  }
+  int32_t bestsum = -1;
+  int besti = 0, bestj = 1;
+  for (int i = 0; i < m; ++i) {
+    const int ai = cand_a(cs, i);
+    for (int j = i + 1; j < m; ++j) {
+      const int aj = cand_a(cs, j);
+      int32_t sum = 0;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        if (k < n) {
+          const int ak = cs.ain[k];
+          sum = wadd(sum, min(min(adist(ai, ak), adist(aj, ak)), fix[k]));
+        }
+      }
+      if (bestsum < 0 || sum < bestsum) {
+        bestsum = sum;
+        besti = i;
+        bestj = j;
+      }
+    }
+  }
+  a0 = cand_a(cs, besti);
+  a1 = cand_a(cs, bestj);
+}
+
+struct EncodedBlock {
+  uint64_t lo, hi;
+};
+
+// s2tc_encode_block<> (s2tc_algorithm.cpp:872-1108) for one block.
+// `prev_a1` is the second alpha endpoint left behind by the previous block of
+// the same image (used only by a single-texel DXT5 block without random
+// candidates); the return value is this block's leftover for the next one.
+template <int DXT, bool NORMAL, int REFINE>
+__device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* rnd, int prev_a1,
+                            EncodedBlock& out) {
+  constexpr bool TRANS = DXT == DXT1;
+  C3 c0, c1;
+  int a0 = 0, a1 = 0;
+  if (!NORMAL) {
+    // darkest / brightest by distance to black (:879-935)
+    const C3 black{0, 0, 0};
+    int32_t dmin = 0x7FFFFFFF, dmax = 0;
+    c0 = C3{31, 63, 31};
+    c1 = black;
+    if (DXT == DXT5) a0 = a1 = texel_a(bt.px[0]);
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        if (x >= bt.w || y >= bt.h) continue;
+        uint32_t t = bt.px[y * 4 + x];
+        if (DXT == DXT1 && (t >> 24) == 0) continue;
+        C3 c = texel_c3(t);
+        int32_t d = cdist<kMetric>(c, black);
+        if (d > dmax) { dmax = d; c1 = c; }
+        if (d < dmin) { dmin = d; c0 = c; }
+        if (DXT == DXT5) {
+          int a = texel_a(t);
+          if (a != 255) {
+            if (a > a1) a1 = a;
+            if (a < a0) a0 = a;
+          }
+        }
+      }
+  } else {
+    Candidates cs;
+    cs.n = 0;
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        if (x >= bt.w || y >= bt.h) continue;
+        uint32_t t = bt.px[y * 4 + x];
+        if (DXT == DXT1 && (t >> 24) == 0) continue;
+        cs.in[cs.n] = texel_c3(t);
+        cs.ain[cs.n] = texel_a(t);
+        cs.n++;
+      }
+    if (cs.n == 0) {
+      cs.n = 1;
+      cs.in[0] = C3{0, 0, 0};
+      cs.ain[0] = 0;
+    }
+    int m = cs.n;
+    cs.nr = 0;
+    cs.rnd = rnd;
+    cs.stride = DXT == DXT5 ? 4 : 3;
+    if (nrandom > 0) {
+      C3 lo = cs.in[0], hi = cs.in[0];
+      int alo = DXT == DXT5 ? cs.ain[0] : 0, ahi = alo;
+      for (int k = 1; k < cs.n; ++k) {
+        lo.r = min(lo.r, cs.in[k].r); lo.g = min(lo.g, cs.in[k].g); lo.b = min(lo.b, cs.in[k].b);
+        hi.r = max(hi.r, cs.in[k].r); hi.g = max(hi.g, cs.in[k].g); hi.b = max(hi.b, cs.in[k].b);
+        if (DXT == DXT5) { alo = min(alo, cs.ain[k]); ahi = max(ahi, cs.ain[k]); }
+      }
+      cs.lo = lo;
+      cs.lr = hi.r - lo.r + 1; cs.lg = hi.g - lo.g + 1; cs.lb = hi.b - lo.b + 1;
+      cs.alo = alo; cs.la = ahi - alo + 1;
+      cs.nr = nrandom;
+      m = cs.n + nrandom;
+    } else if (cs.n == 1) {
+      // single input (:996-1001): the colour is duplicated; the reference's
+      // second alpha candidate is whatever the previous block left in that slot
+      cs.in[1] = cs.in[0];
+      cs.ain[1] = prev_a1 >= 0 ? prev_a1 : cs.ain[0];
+      cs.n = 2;
+      m = 2;
+    }
+    reduce_rgb(cs, m, c0, c1);
+    if (DXT == DXT5) reduce_alpha(cs, m, a0, a1);
+  }
+
+  // equal endpoints are bumped apart (:1009-1027)
+  if (c3_eq(c0, c1)) c1 = (c0.r == 31 && c0.g == 63 && c0.b == 31) ? c3_prev(c1) : c3_next(c1);
+  if (DXT == DXT5 && a0 == a1) {
+    if (a0 == 255) --a1; else ++a1;
+  }
+
+  uint32_t cbits = colour_refine<kMetric, TRANS, REFINE>(bt, c0, c1);
+  const uint64_t colour = uint64_t(pack565(c0)) | (uint64_t(pack565(c1)) << 16) | (uint64_t(cbits) << 32);
+  int leftover = a1;
+  if (DXT == DXT1) {
+    out.lo = colour;
+    out.hi = 0;
+  } else if (DXT == DXT3) {
+    uint64_t ab = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if ((i & 3) < bt.w && (i >> 2) < bt.h) ab |= uint64_t(texel_a(bt.px[i]) & 15) << (4 * i);
+    out.lo = ab;
+    out.hi = colour;
+  } else {
+    uint64_t abits = alpha_refine<REFINE>(bt, a0, a1, leftover);
+    out.lo = uint64_t(a0) | (uint64_t(a1) << 8) | (abits << 16);
+    out.hi = colour;
+  }
+  return leftover;
+}
+
+__device__ __forceinline__ void load_block(const uint32_t* __restrict__ t565, int width, int height, int bx, int by,
+                                           BlockTexels& bt) {
+  bt.w = min(4, width - bx * 4);
+  bt.h = min(4, height - by * 4);
+  const uint32_t* p = t565 + size_t(by) * 4 * width + size_t(bx) * 4;
+#pragma unroll
+  for (int y = 0; y < 4; ++y)
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+      bt.px[y * 4 + x] = (x < bt.w && y < bt.h) ? __ldg(p + size_t(y) * width + x) : 0u;
+}
+
+template <int DXT, bool NORMAL, int REFINE>
+__global__ void __launch_bounds__(128) k_encode(EncodeArgs a) {
+  const long long bl = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // block within this launch
+  if (bl >= (long long)a.bw * a.nby) return;
+  const long long b = (long long)a.by0 * a.bw + bl;                         // block within the image
+  const int by = int(b / a.bw), bx = int(b % a.bw);
+  BlockTexels bt;
+  load_block(a.t565, a.width, a.height, bx, by, bt);
+  const int per_block = a.nrandom > 0 ? a.nrandom * (DXT == DXT5 ? 4 : 3) : 0;
+  const uint32_t* rnd = a.rnd ? a.rnd + (size_t)bl * per_block : nullptr;
+  int prev_a1 = -1;
+  if (DXT == DXT5 && NORMAL && a.nrandom <= 0 && bt.w == 1 && bt.h == 1) {
+    // The reference encodes blocks in raster order into the same stack
+    // frame; a single-texel DXT5 block reads its second alpha candidate from
+    // a slot it never writes, i.e. the value the previous block left there
+    // (s2tc_algorithm.cpp:876, 996-1001).  That block is re-encoded here to
+    // recover it.
+    if (b > 0) {
+      const int pby = int((b - 1) / a.bw), pbx = int((b - 1) % a.bw);
+      BlockTexels pt;
+      load_block(a.t565, a.width, a.height, pbx, pby, pt);
+      EncodedBlock scratch;
+      prev_a1 = encode_block<DXT, NORMAL, REFINE>(pt, a.nrandom, nullptr, -1, scratch);
+    } else {
+      prev_a1 = a.prev_a1_first;
+    }
+  }
+  EncodedBlock eb;
+  const int leftover = encode_block<DXT, NORMAL, REFINE>(bt, a.nrandom, rnd, prev_a1, eb);
+  if (a.leftover_out && b == (long long)a.bw * a.bh - 1) *a.leftover_out = leftover;
+  uint8_t* o = a.dst + (size_t)by * a.pitch + (size_t)bx * (DXT == DXT1 ? 8 : 16);
+  if (a.aligned) {
+    if (DXT == DXT1) {
+      *reinterpret_cast<uint64_t*>(o) = eb.lo;
+    } else {
+      *reinterpret_cast<ulonglong2*>(o) = make_ulonglong2(eb.lo, eb.hi);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) o[i] = uint8_t(eb.lo >> (8 * i));
+    if (DXT != DXT1) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) o[8 + i] = uint8_t(eb.hi >> (8 * i));
+    }
+  }
+}
+
+template <int DXT, bool NORMAL>
+cudaError_t launch_r(const EncodeArgs& a, int refine, cudaStream_t s) {
+  const long long nb = (long long)a.bw * a.nby;
+  if (nb == 0) return cudaSuccess;
+  const int threads = 128;
+  const unsigned grid = unsigned((nb + threads - 1) / threads);
+  switch (refine) {
+    case RF_NEVER: k_encode<DXT, NORMAL, RF_NEVER><<<grid, threads, 0, s>>>(a); break;
+    case RF_LOOP: k_encode<DXT, NORMAL, RF_LOOP><<<grid, threads, 0, s>>>(a); break;
+    default: k_encode<DXT, NORMAL, RF_ALWAYS><<<grid, threads, 0, s>>>(a); break;
+  }
+  return cudaGetLastError();
+}
+
+template <int DXT>
+cudaError_t launch_d(const EncodeArgs& a, bool normal, int refine, cudaStream_t s) {
+  // NORMALMAP never uses the quick selection (s2tc_algorithm.cpp:1127-1143)
+  if (normal || kMetric == CD_NORMALMAP) return launch_r<DXT, true>(a, refine, s);
+  return launch_r<DXT, (kMetric == CD_NORMALMAP)>(a, refine, s);
+}
+
+}  // namespace
+
+#define S2TC_CAT2(a, b) a##b
+#define S2TC_CAT(a, b) S2TC_CAT2(a, b)
+
+cudaError_t S2TC_CAT(launch_encode_m, S2TC_METRIC)(const EncodeArgs& a, int dxt, bool normal, int refine,
+                                                   cudaStream_t s) {
+  switch (dxt) {
+    case DXT1: return launch_d<DXT1>(a, normal, refine, s);
+    case DXT3: return launch_d<DXT3>(a, normal, refine, s);
+    default: return launch_d<DXT5>(a, normal, refine, s);
+  }
+}
+
+}  // namespace s2tc

@@ -1,0 +1,334 @@
+// s2tc_device.cuh -- device-side building blocks of the S2TC block encoder:
+// 5:6:5 colour helpers, the eight colour-distance metrics, index passes,
+// refinement and block packing.  Everything here is integer arithmetic with
+// 32-bit wrap-around except the NORMALMAP and SRGB_MIXED float steps, which use
+// explicitly rounded single-precision intrinsics (no fused multiply-add) so the
+// results equal the reference's x86-64 SSE code.
+//
+// Reference: s2tc_algorithm.cpp (divVerent/s2tc); line numbers are cited per
+// function.
+#pragma once
+#include <cstdint>
+
+#include "s2tc_types.h"
+
+namespace s2tc {
+
+// ----------------------------------------------------------------- colours
+
+struct C3 {
+  int r, g, b;
+};
+
+__device__ __forceinline__ C3 texel_c3(uint32_t t) {
+  return C3{int(t & 0xFF), int((t >> 8) & 0xFF), int((t >> 16) & 0xFF)};
+}
+__device__ __forceinline__ int texel_a(uint32_t t) { return int(t >> 24); }
+
+__device__ __forceinline__ bool c3_eq(C3 a, C3 b) { return a.r == b.r && a.g == b.g && a.b == b.b; }
+// Lexicographic r,g,b order, which is the numeric order of the 5:6:5 word
+// (s2tc_algorithm.cpp:70-81).
+__device__ __forceinline__ int c3_key(C3 a) { return (a.r << 11) | (a.g << 5) | a.b; }
+__device__ __forceinline__ bool c3_lt(C3 a, C3 b) { return c3_key(a) < c3_key(b); }
+// Wrapping step through the 5:6:5 space (s2tc_algorithm.cpp:82-131).
+__device__ __forceinline__ C3 c3_from_key(int k) { return C3{(k >> 11) & 31, (k >> 5) & 63, k & 31}; }
+__device__ __forceinline__ C3 c3_next(C3 a) { return c3_from_key((c3_key(a) + 1) & 0xFFFF); }
+__device__ __forceinline__ C3 c3_prev(C3 a) { return c3_from_key((c3_key(a) + 0xFFFF) & 0xFFFF); }
+
+// ----------------------------------------------------------------- metrics
+// s2tc_algorithm.cpp:215-361.  `a` is the first argument of the reference's
+// call; SRGB is not symmetric in its arguments.
+
+__device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return int32_t(uint32_t(a) + uint32_t(b)); }
+__device__ __forceinline__ int32_t wmul(int32_t a, int32_t b) { return int32_t(uint32_t(a) * uint32_t(b)); }
+template <int N>
+__device__ __forceinline__ int32_t shrr(int32_t a) { return wadd(a, 1 << (N - 1)) >> N; }
+
+__device__ __forceinline__ int srgb_luma(int r, int g, int b) {
+  // (int)(sqrtf((float)y) + 0.5f), s2tc_algorithm.cpp:285-296
+  int y = 37 * (r * r * 84 + g * g * 72 + b * b * 28);
+  float f = __fadd_rn(__fsqrt_rn(__int2float_rn(y)), 0.5f);
+  return __float2int_rz(f);
+}
+
+struct NUnit {
+  float x, y, z;
+};
+// Unit vector of a normal-map texel (s2tc_algorithm.cpp:320-341).
+__device__ __forceinline__ NUnit nm_unit(C3 c) {
+  NUnit v;
+  v.x = __fsub_rn(__fmul_rn(__fdiv_rn(__int2float_rn(c.r), 31.0f), 2.0f), 1.0f);
+  v.y = __fsub_rn(__fmul_rn(__fdiv_rn(__int2float_rn(c.g), 63.0f), 2.0f), 1.0f);
+  v.z = __fsub_rn(__fmul_rn(__fdiv_rn(__int2float_rn(c.b), 31.0f), 2.0f), 1.0f);
+  float n = __fadd_rn(__fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)), __fmul_rn(v.z, v.z));
+  if (n > 0.0f) {
+    n = __fdiv_rn(1.0f, __fsqrt_rn(n));
+    v.x = __fmul_rn(v.x, n);
+    v.y = __fmul_rn(v.y, n);
+    v.z = __fmul_rn(v.z, n);
+  }
+  return v;
+}
+// 100000 * |vb - va|^2 truncated to int (s2tc_algorithm.cpp:343-352).
+__device__ __forceinline__ int32_t nm_dist(NUnit a, NUnit b) {
+  float t = __fsub_rn(b.x, a.x);
+  float s = __fmul_rn(t, t);
+  t = __fsub_rn(b.y, a.y);
+  s = __fadd_rn(s, __fmul_rn(t, t));
+  t = __fsub_rn(b.z, a.z);
+  s = __fadd_rn(s, __fmul_rn(t, t));
+  return __float2int_rz(__fmul_rn(100000.0f, s));
+}
+
+template <int METRIC>
+__device__ __forceinline__ int32_t cdist(C3 a, C3 b) {
+  if (METRIC == CD_AVG) {
+    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
+    return ((dr * dr) << 2) + dg * dg + ((db * db) << 2);
+  } else if (METRIC == CD_W0AVG) {
+    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
+    return dr * dr + dg * dg + db * db;
+  } else if (METRIC == CD_WAVG) {
+    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
+    return ((dr * dr) << 2) + ((dg * dg) << 2) + db * db;
+  } else if (METRIC == CD_YUV || METRIC == CD_RGB) {
+    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
+    int y = METRIC == CD_YUV ? dr * 60 + dg * 59 + db * 22 : dr * 42 + dg * 72 + db * 14;
+    int u = dr * 202 - y, v = db * 202 - y;
+    return wadd(wadd(wmul(y, y) << 1, shrr<3>(wmul(u, u))), shrr<4>(wmul(v, v)));
+  } else if (METRIC == CD_SRGB) {
+    int dr = a.r * a.r - b.r * b.r, dg = a.g * a.g - b.g * b.g, db = a.b * a.b - b.b * b.b;
+    int y = dr * 84 + dg * 72 + db * 28;
+    int u = dr * 409 - y, v = db * 409 - y;
+    int32_t sy = wmul(shrr<3>(y), shrr<4>(y));
+    int32_t su = wmul(shrr<3>(u), shrr<4>(u));
+    int32_t sv = wmul(shrr<3>(v), shrr<4>(v));
+    return wadd(wadd(shrr<4>(sy), shrr<8>(su)), shrr<9>(sv));
+  } else if (METRIC == CD_SRGB_MIXED) {
+    int ay = srgb_luma(a.r, a.g, a.b), by = srgb_luma(b.r, b.g, b.b);
+    int y = ay - by;
+    int u = (a.r * 191 - ay) - (b.r * 191 - by);
+    int v = (a.b * 191 - ay) - (b.b * 191 - by);
+    return wadd(wadd(wmul(y, y) << 3, shrr<1>(wmul(u, u))), shrr<2>(wmul(v, v)));
+  } else {  // CD_NORMALMAP
+    return nm_dist(nm_unit(a), nm_unit(b));
+  }
+}
+
+__device__ __forceinline__ int32_t adist(int a, int b) { return (a - b) * (a - b); }
+
+// ------------------------------------------------------ block texel access
+
+// One 4x4 (or edge w x h) block held as 16 texel words, slot y*4+x.  Each word
+// is r | g<<8 | b<<16 | a<<24 with r,b in 0..31, g in 0..63 and a quantised to
+// the format's alpha bits.
+struct BlockTexels {
+  uint32_t px[16];
+  int w, h;
+};
+
+// ------------------------------------------------------ colour index pass
+
+struct ColourAcc {
+  int n0, n1;
+  int s0r, s0g, s0b, s1r, s1g, s1b;
+};
+
+// s2tc_algorithm.cpp:582-643 (colour, two references): nearest endpoint per
+// texel, ties to endpoint 0; DXT1 alpha-0 texels take index 3.  Visits x-outer,
+// y-inner like the reference; the order matters only for the score sum, which
+// is order-independent, so any order gives the same result.
+template <int METRIC, bool TRANS, bool ACC>
+__device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, C3 r0, C3 r1, uint32_t& bits,
+                                                ColourAcc& acc) {
+  uint32_t score = 0;
+  bits = 0;
+  if (ACC) acc = ColourAcc{0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int x = i & 3, y = i >> 2;
+    if (x >= bt.w || y >= bt.h) continue;
+    uint32_t t = bt.px[i];
+    if (TRANS && (t >> 24) == 0) {
+      bits |= 3u << (2 * i);
+      continue;
+    }
+    C3 c = texel_c3(t);
+    int32_t d0 = cdist<METRIC>(c, r0), d1 = cdist<METRIC>(c, r1);
+    const bool one = d1 < d0;
+    if (ACC) {
+      if (one) {
+        acc.n1++;
+        acc.s1r += c.r; acc.s1g += c.g; acc.s1b += c.b;
+      } else {
+        acc.n0++;
+        acc.s0r += c.r; acc.s0g += c.g; acc.s0b += c.b;
+      }
+    }
+    bits |= uint32_t(one) << (2 * i);
+    score += uint32_t(one ? d1 : d0);
+  }
+  return score;
+}
+
+__device__ __forceinline__ int rmean(int s, int n) { return ((s << 1) + n) / (n << 1); }
+
+// s2tc_algorithm.cpp:542-551
+__device__ __forceinline__ bool colour_means(const ColourAcc& a, C3& c0, C3& c1) {
+  if (!a.n0 && !a.n1) return false;
+  if (a.n0) c0 = C3{rmean(a.s0r, a.n0) & 31, rmean(a.s0g, a.n0) & 63, rmean(a.s0b, a.n0) & 31};
+  if (a.n1) c1 = C3{rmean(a.s1r, a.n1) & 31, rmean(a.s1g, a.n1) & 63, rmean(a.s1b, a.n1) & 31};
+  return true;
+}
+
+// Equal-endpoint fix and canonical order (s2tc_algorithm.cpp:796-813).
+template <bool TRANS>
+__device__ __forceinline__ void colour_finish(uint32_t& bits, C3& c0, C3& c1) {
+  if (c3_eq(c0, c1)) {
+    c1 = (c0.r == 31 && c0.g == 63 && c0.b == 31) ? c3_prev(c1) : c3_next(c1);
+    // indices other than 1 become 0
+    uint32_t lo = bits & 0x55555555u, hi = (bits >> 1) & 0x55555555u;
+    bits = lo & ~hi;
+  }
+  if (TRANS ? c3_lt(c1, c0) : c3_lt(c0, c1)) {
+    C3 t = c0; c0 = c1; c1 = t;
+    // xor bit 0 of every index whose bit 1 is clear
+    uint32_t hi = (bits >> 1) & 0x55555555u;
+    bits ^= ~hi & 0x55555555u;
+  }
+}
+
+// Colour refinement NEVER / ALWAYS / LOOP (s2tc_algorithm.cpp:767-860).
+template <int METRIC, bool TRANS, int REFINE>
+__device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, C3& c0, C3& c1) {
+  uint32_t bits;
+  ColourAcc acc;
+  if (REFINE == RF_NEVER) {
+    if (TRANS ? c3_lt(c1, c0) : c3_lt(c0, c1)) {
+      C3 t = c0; c0 = c1; c1 = t;
+    }
+    colour_pass<METRIC, TRANS, false>(bt, c0, c1, bits, acc);
+    return bits;
+  } else if (REFINE == RF_LOOP) {
+    C3 n0 = c0, n1 = c1;
+    uint32_t best = 0x7FFFFFFFu;
+    bits = 0;
+    for (;;) {
+      uint32_t b2;
+      uint32_t s2 = colour_pass<METRIC, TRANS, true>(bt, n0, n1, b2, acc);
+      if (!(s2 < best)) break;
+      bits = b2;
+      best = s2;
+      c0 = n0;
+      c1 = n1;
+      if (!colour_means(acc, n0, n1)) break;
+    }
+  } else {
+    colour_pass<METRIC, TRANS, true>(bt, c0, c1, bits, acc);
+    colour_means(acc, c0, c1);
+  }
+  colour_finish<TRANS>(bits, c0, c1);
+  return bits;
+}
+
+// --------------------------------------------------------- DXT5 alpha pass
+
+// s2tc_algorithm.cpp:582-643 with bpp=3 and the 0/255 fixed points.
+template <bool ACC>
+__device__ __forceinline__ uint32_t alpha_pass(const BlockTexels& bt, int r0, int r1, uint64_t& bits,
+                                               int& n0, int& n1, int& s0, int& s1) {
+  uint32_t score = 0;
+  bits = 0;
+  if (ACC) n0 = n1 = s0 = s1 = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int x = i & 3, y = i >> 2;
+    if (x >= bt.w || y >= bt.h) continue;
+    int a = int(bt.px[i] >> 24);
+    int32_t bd = adist(a, r0), d1 = adist(a, r1);
+    int best = 0;
+    if (d1 < bd) { bd = d1; best = 1; }
+    int32_t dz = a * a;
+    if (dz <= bd) {
+      bits |= uint64_t(6) << (3 * i);
+      score += uint32_t(dz);
+      continue;
+    }
+    int32_t df = (255 - a) * (255 - a);
+    if (df <= bd) {
+      bits |= uint64_t(7) << (3 * i);
+      score += uint32_t(df);
+      continue;
+    }
+    if (ACC) {
+      if (best) { n1++; s1 += a; } else { n0++; s0 += a; }
+    }
+    bits |= uint64_t(best) << (3 * i);
+    score += uint32_t(bd);
+  }
+  return score;
+}
+
+// s2tc_algorithm.cpp:673-705
+__device__ __forceinline__ void alpha_finish(uint64_t& bits, int& a0, int& a1) {
+  if (a0 == a1) {
+    if (a0 == 255) --a1; else ++a1;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (((bits >> (3 * i)) & 7) == 1) bits &= ~(uint64_t(7) << (3 * i));
+  }
+  if (a1 < a0) {
+    int t = a0; a0 = a1; a1 = t;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      uint64_t v = (bits >> (3 * i)) & 7, nv;
+      if (v == 0) nv = 1;
+      else if (v == 1) nv = 0;
+      else if (v >= 6) nv = v;
+      else nv = 7 - v;
+      bits = (bits & ~(uint64_t(7) << (3 * i))) | (nv << (3 * i));
+    }
+  }
+}
+
+// s2tc_algorithm.cpp:645-765.  Returns the value of the second endpoint that a
+// following single-texel block would read (see encode_block).
+template <int REFINE>
+__device__ __forceinline__ uint64_t alpha_refine(const BlockTexels& bt, int& a0, int& a1, int& leftover) {
+  uint64_t bits = 0;
+  int n0, n1, s0, s1;
+  if (REFINE == RF_NEVER) {
+    leftover = a1;
+    if (a1 < a0) { int t = a0; a0 = a1; a1 = t; }
+    alpha_pass<false>(bt, a0, a1, bits, n0, n1, s0, s1);
+    return bits;
+  } else if (REFINE == RF_LOOP) {
+    int x0 = a0, x1 = a1;
+    uint32_t best = 0x7FFFFFFFu;
+    for (;;) {
+      uint64_t b2;
+      uint32_t s2 = alpha_pass<true>(bt, x0, x1, b2, n0, n1, s0, s1);
+      if (!(s2 < best)) break;
+      bits = b2;
+      best = s2;
+      a0 = x0;
+      a1 = x1;
+      if (!n0 && !n1) break;
+      if (n0) x0 = rmean(s0, n0) & 255;
+      if (n1) x1 = rmean(s1, n1) & 255;
+    }
+  } else {
+    alpha_pass<true>(bt, a0, a1, bits, n0, n1, s0, s1);
+    if (n0) a0 = rmean(s0, n0) & 255;
+    if (n1) a1 = rmean(s1, n1) & 255;
+  }
+  alpha_finish(bits, a0, a1);
+  leftover = a1;
+  return bits;
+}
+
+// ------------------------------------------------------------------ packing
+
+__device__ __forceinline__ uint32_t pack565(C3 c) { return uint32_t((c.r << 11) | (c.g << 5) | c.b); }
+
+}  // namespace s2tc
