@@ -1,0 +1,402 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 S2TC encoder (one JSON line on rank 0).
+
+Default workload: one 4096x4096 RGBA8 image -> DXT5 with SRGB_MIXED distance,
+the all-16 endpoint search (RANDOM_COLORS=0) and LOOP refinement, SIMPLE
+dither.  A step is one compression of one image.
+
+* ``value``: texels/s with the inputs resident in HBM (s2tc_gpu_compress on
+  device buffers), timed with CUDA events on the launching stream over K
+  back-to-back steps.  The inputs rotate over four distinct 64 MB images
+  (256 MB > the 129 MB L2), so every step reads its input cold.
+* ``e2e``: the same metric through the reference-compatible C entry point
+  tx_compress_dxtn with pinned host buffers (upload, kernels, download, sync).
+* ``roofline``: the dominant kernel's algorithmic bytes per launch over its
+  average launch time (library-recorded CUDA events on the launching stream)
+  against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the CPU port of the reference encoder (oracle/) on one
+  core, on the first workload image; its bytes are also compared with the GPU
+  output (``bit_exact``).
+
+``--impl reference`` times the reference's CPU implementation instead (the
+reference library compiled from its sources when present, else the CPU port),
+one worker process per host core, each compressing a band of the workload.
+
+Multi-GPU (torchrun): every rank compresses its own images (replicas, no
+collective on the data path); value = all ranks' texels / the slowest rank's
+time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "texels/s"
+NIMG = 4
+
+WORKLOADS = {
+    "value_noise_4096_dxt5_srgb_mixed_all16_loop": dict(
+        w=4096, h=4096, sc=4, fmt=0x83F3, dither=1, metric=3, nrandom=0, refine=2, gen="value_noise", seed=2),
+    "plain_1024_dxt1_wavg_quick_always": dict(
+        w=1024, h=1024, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
+    "plain_8192_dxt1_wavg_quick_always": dict(
+        w=8192, h=8192, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
+    "normal_map_2048_dxt1_normalmap_rand64_loop": dict(
+        w=2048, h=2048, sc=3, fmt=0x83F1, dither=1, metric=7, nrandom=64, refine=2, gen="normal", seed=4),
+}
+DEFAULT_WORKLOAD = "value_noise_4096_dxt5_srgb_mixed_all16_loop"
+FMT_NAMES = {0x83F0: "DXT1(RGB)", 0x83F1: "DXT1", 0x83F2: "DXT3", 0x83F3: "DXT5"}
+
+
+def make_image(wl: dict, seed: int, rows: int | None = None) -> np.ndarray:
+    """Workload image (flattened); with `rows`, an image of the same recipe
+    and width but only that many rows."""
+    from s2tc_gb300 import workloads
+    w, h = wl["w"], wl["h"] if rows is None else rows
+    if wl["gen"] == "value_noise":
+        img = workloads.value_noise_rgba(seed, w, h)
+    elif wl["gen"] == "plain":
+        img = workloads.plain_rgba(seed, w, h)
+    else:
+        img = workloads.normal_map(seed, w, h)
+    return np.ascontiguousarray(img.reshape(-1))
+
+
+def algorithmic_bytes_per_texel(wl: dict) -> float:
+    """Input read once + output written once (the 5:6:5 intermediate is not
+    counted: a fused encoder would not materialise it)."""
+    return wl["sc"] + (8 if wl["fmt"] in (0x83F0, 0x83F1) else 16) / 16.0
+
+
+def config_dict(wl_name: str, wl: dict) -> dict:
+    import s2tc_gb300 as s2
+    return {"workload": wl_name, "width": wl["w"], "height": wl["h"], "srccomps": wl["sc"],
+            "format": FMT_NAMES[wl["fmt"]], "dither": s2.DITHER_NAMES[wl["dither"]],
+            "colordist": s2.COLORDIST_NAMES[wl["metric"]], "random_colors": wl["nrandom"],
+            "refine": s2.REFINE_NAMES[wl["refine"]],
+            "l2": f"inputs rotate over {NIMG} resident images larger in total than the 129 MB L2"}
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """Samples SM clock and clock-event reasons through NVML (read only)
+    while running."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, cuda_index: int = 0):
+        self.samples: list[int] = []
+        self.reasons = 0
+        self.max_mhz = None
+        self._stop = threading.Event()
+        self._nvml = None
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            handle = ctypes.c_void_p()
+            ok = False
+            try:
+                import torch
+                p = torch.cuda.get_device_properties(cuda_index)
+                bus = f"{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0".encode()
+                ok = nv.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(handle)) == 0
+            except Exception:
+                ok = False
+            if not ok and nv.nvmlDeviceGetHandleByIndex_v2(cuda_index, ctypes.byref(handle)) != 0:
+                return
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = mx.value
+            try:
+                self._reasons_fn = nv.nvmlDeviceGetCurrentClocksEventReasons
+            except AttributeError:
+                self._reasons_fn = nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            self._nvml, self._h = nv, handle
+        except OSError:
+            self._nvml = None
+
+    def _run(self):
+        nv, h = self._nvml, self._h
+        mhz, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self._stop.is_set():
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0:
+                self.samples.append(mhz.value)
+            if self._reasons_fn(h, ctypes.byref(rs)) == 0:
+                self.reasons |= rs.value
+            time.sleep(0.002)
+
+    def __enter__(self):
+        if self._nvml is not None:
+            self._t = threading.Thread(target=self._run, daemon=True)
+            self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._nvml is not None:
+            self._t.join()
+
+    def summary(self) -> dict:
+        if self._nvml is None or not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0,
+                    "note": "NVML unavailable" if self._nvml is None else "no samples"}
+        return {"sm_mhz": statistics.median(self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": [n for b, n in self.REASONS.items() if self.reasons & b],
+                "samples": len(self.samples)}
+
+
+# --------------------------------------------------------------- CPU legs
+
+_WORKER_IMAGES: dict = {}
+
+
+def _cpu_worker(args):
+    """One CPU compression of a workload band (runs in a spawned process);
+    returns (seconds, output).  The image is made once per process."""
+    wl_name, rows, use_ref, seed = args
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    wl = WORKLOADS[wl_name]
+    key = (wl_name, rows)
+    if key not in _WORKER_IMAGES:
+        _WORKER_IMAGES[key] = make_image(wl, wl["seed"], None if rows == wl["h"] else rows)
+    img = _WORKER_IMAGES[key]
+    enc = pyoracle.Reference() if use_ref else pyoracle.Oracle()
+    t0 = time.perf_counter()
+    out = enc.compress(wl["sc"], wl["w"], rows, img, wl["fmt"], wl["dither"], wl["metric"], wl["nrandom"],
+                       wl["refine"], seed=seed)
+    return time.perf_counter() - t0, out, os.getpid()
+
+
+def reference_kind() -> tuple[bool, str]:
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    if pyoracle.Reference.available():
+        return True, "reference"
+    pyoracle.ensure_built()
+    return False, "port"
+
+
+def run_reference_arm(args, wl_name: str, wl: dict) -> None:
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    use_ref, kind = reference_kind()
+    cores = os.cpu_count() or 1
+    # a band of rows sized to about a second of single-core work per step
+    rows = min(wl["h"], 1024 if wl["metric"] in (3, 7) or wl["nrandom"] >= 0 else 4096)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        times = []
+        for step in range(args.warmup + args.steps):
+            # all workers compress concurrently; the step lasts as long as the
+            # slowest, or the whole map when a worker ran two tasks in a row
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, [(wl_name, rows, use_ref, 1 + step)] * cores, chunksize=1)
+            wall = time.perf_counter() - t0
+            if step >= args.warmup:
+                concurrent = len({r[2] for r in res}) == cores
+                times.append(max(r[0] for r in res) if concurrent else wall)
+    texels = cores * wl["w"] * rows
+    total = sum(times)
+    value = texels * len(times) / total
+    sample = f"{cores} processes, each the first {rows} rows ({wl['w']}x{rows}) of the workload image per step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "config": config_dict(wl_name, wl),
+            "cpu_baseline": {"value": value, "unit": "texels/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "texels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_port(wl_name: str, wl: dict, gpu_out0: np.ndarray | None) -> dict:
+    """The CPU port on one core, on the full first workload image."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        dt, out, _ = pool.map(_cpu_worker, [(wl_name, wl["h"], False, 1)])[0]
+    res = {"value": wl["w"] * wl["h"] / dt, "unit": "texels/s", "cores": 1, "kind": "port",
+           "sample": f"one full {wl['w']}x{wl['h']} image, single thread ({dt:.2f} s)"}
+    if gpu_out0 is not None:
+        res["bit_exact"] = bool(np.array_equal(out, gpu_out0))
+    return res
+
+
+# ------------------------------------------------------------------- GPU arm
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU port leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.warmup < 3 and args.impl == "gb300":
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference_arm(args, args.workload, wl)
+        return
+
+    import torch
+    import s2tc_gb300 as s2
+    from s2tc_gb300 import build as s2build
+    if not s2.LIB_PATH.exists():
+        s2build.build_library()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    w, h, sc, fmt = wl["w"], wl["h"], wl["sc"], wl["fmt"]
+    npx = w * h
+    out_bytes = s2.compressed_size(w, h, fmt)
+    opt = s2.options(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+    images = [make_image(wl, wl["seed"] + 100 * rank + i) for i in range(NIMG)]
+    d_src = [torch.from_numpy(im).cuda() for im in images]
+    d_dst = [torch.empty(out_bytes, dtype=torch.uint8, device="cuda") for _ in range(NIMG)]
+    d_rand = None
+    nwords = s2.rand_words(w, h, fmt, opt)
+    if nwords:
+        # replayed rand() words for one image, reused by every step
+        sys.path.insert(0, str(ROOT / "oracle"))
+        rng = np.random.default_rng(9)
+        d_rand = torch.from_numpy(rng.integers(0, 2**31, nwords, dtype=np.int64).astype(np.uint32)).cuda()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step(i, rand=d_rand):
+        s2.gpu_compress(sc, w, h, d_src[i % NIMG], fmt, d_dst[i % NIMG], opt=opt, d_rand=rand, stream=sp)
+
+    # first warm-up step: image 0 with libc rand() replayed from srand(1), the
+    # output the CPU leg checks; the timed steps reuse one stored rand stream
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    pyoracle.srand(1)
+    step(0, None)
+    s2.gpu_synchronize(sp)
+    out0 = d_dst[0].cpu().numpy()
+    for i in range(1, args.warmup):
+        step(i)
+    s2.gpu_synchronize(sp)
+
+    # --- device-resident timed region
+    s2.set_timing(True)
+    l0 = s2.kernel_launches()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for i in range(args.steps):
+            step(i)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = s2.kernel_launches() - l0
+    dither_ms, encode_ms, calls = s2.stage_ms()
+    s2.set_timing(False)
+    s2.gpu_synchronize(sp)
+    elapsed = ev0.elapsed_time(ev1) / 1000.0
+    if dist is not None:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps * npx / elapsed
+
+    # --- end to end through tx_compress_dxtn with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        s2.set_env(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+        h_src = [torch.from_numpy(im).pin_memory() for im in images]
+        h_dst = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+        lib = s2.load()
+        for i in range(min(args.warmup, 3)):
+            lib.tx_compress_dxtn(sc, w, h, h_src[i % NIMG].data_ptr(), fmt, h_dst.data_ptr(), 0)
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            lib.tx_compress_dxtn(sc, w, h, h_src[i % NIMG].data_ptr(), fmt, h_dst.data_ptr(), 0)
+        t_e2e = time.perf_counter() - t0
+        barrier()
+        if dist is not None:
+            t = torch.tensor([t_e2e], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        e2e = {"value": world * args.steps * npx / t_e2e, "unit": "texels/s",
+               "h2d_bytes_per_step": npx * sc, "d2h_bytes_per_step": out_bytes,
+               "ms_per_step": 1000 * t_e2e / args.steps}
+
+    # --- roofline of the dominant kernel
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_note = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    enc_launch_ms = encode_ms / max(1, calls)
+    dit_launch_ms = dither_ms / max(1, calls)
+    alg_bytes = algorithmic_bytes_per_texel(wl) * npx
+    dominant = "encode" if enc_launch_ms >= dit_launch_ms else "dither"
+    dom_ms = max(enc_launch_ms, dit_launch_ms)
+    achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "peak_source": peak_note, "traffic": None,
+                "stage_ms_per_launch": {"dither": dit_launch_ms, "encode": enc_launch_ms},
+                "note": "the all-pairs search is integer-ALU bound; frac is of the HBM roofline for the "
+                        "algorithmic bytes"}
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            roofline["traffic"] = json.loads(prof.read_text()).get(args.workload, {}).get(dominant)
+        except Exception:
+            pass
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_port(args.workload, wl, out0)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+                "config": config_dict(args.workload, wl), "e2e": e2e, "gpu_launches": launches,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -113,6 +113,17 @@ int s2tc_gpu_synchronize(void *stream);
  * else 3) when the random-candidate search is active, else 0. */
 long long s2tc_rand_words(int width, int height, unsigned int destformat, const s2tc_options *opt);
 
+/* Profiling hook: while enabled, every compression records CUDA events on its
+ * stream before the dither kernel, between the dither and encoder kernels and
+ * after the encoder (up to 4096 calls after each enable).  s2tc_gpu_stage_ms
+ * waits for them and returns the summed stage durations in milliseconds and
+ * the number of calls they cover. */
+int s2tc_gpu_set_timing(int enable);
+int s2tc_gpu_stage_ms(float *dither_ms, float *encode_ms, long long *calls);
+
+/* Number of CUDA kernels this library has launched since it was loaded. */
+long long s2tc_gpu_kernel_launches(void);
+
 /* Text of the last error this thread saw (empty when none). */
 const char *s2tc_last_error(void);
 

@@ -97,6 +97,13 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_gpu_synchronize.restype = c_int
     lib.s2tc_rand_words.argtypes = [c_int, c_int, c_uint, ctypes.POINTER(Options)]
     lib.s2tc_rand_words.restype = c_ll
+    lib.s2tc_gpu_set_timing.argtypes = [c_int]
+    lib.s2tc_gpu_set_timing.restype = c_int
+    lib.s2tc_gpu_stage_ms.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(c_ll)]
+    lib.s2tc_gpu_stage_ms.restype = c_int
+    lib.s2tc_gpu_kernel_launches.argtypes = []
+    lib.s2tc_gpu_kernel_launches.restype = c_ll
     lib.s2tc_last_error.argtypes = []
     lib.s2tc_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -109,7 +116,9 @@ EXPORTED_SYMBOLS = (
     "tx_compress_dxtn", "fetch_2d_texel_rgb_dxt1", "fetch_2d_texel_rgba_dxt1",
     "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5", "rgb565_image",
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
-    "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_last_error",
+    "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
+    "s2tc_gpu_kernel_launches",
+    "s2tc_last_error",
 )
 
 
@@ -217,6 +226,27 @@ def gpu_compress(srccomps: int, width: int, height: int, d_src, destformat: int,
                                   ctypes.byref(opt), rnd_p, stream)
     if st != S2TC_OK:
         raise S2tcError(f"s2tc_gpu_compress failed ({st}): {last_error()}")
+
+
+def set_timing(enable: bool) -> None:
+    st = load().s2tc_gpu_set_timing(1 if enable else 0)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_set_timing failed ({st}): {last_error()}")
+
+
+def stage_ms() -> tuple[float, float, int]:
+    """(dither_ms, encode_ms, calls): summed stage durations of the
+    compressions since set_timing(True), from CUDA events recorded on their
+    stream."""
+    a, b, n = ctypes.c_float(), ctypes.c_float(), ctypes.c_longlong()
+    st = load().s2tc_gpu_stage_ms(ctypes.byref(a), ctypes.byref(b), ctypes.byref(n))
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_stage_ms failed ({st}): {last_error()}")
+    return a.value, b.value, n.value
+
+
+def kernel_launches() -> int:
+    return int(load().s2tc_gpu_kernel_launches())
 
 
 def gpu_synchronize(stream: int | None = None) -> None:

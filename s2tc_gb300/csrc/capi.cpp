@@ -80,6 +80,11 @@ struct Context {
   bool ready = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t arena_free = nullptr;  // recorded after the last work that used the arena
+  // s2tc_gpu_set_timing: per-stage CUDA events of the last kTimingSlots calls
+  static constexpr int kTimingSlots = 4096;
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;   // 3 per slot: before dither, between, after encode
+  long long timed_calls = 0;
   DevBuf src, t565, dst, scratch, rnd, err;
   PinnedBuf host_rnd, host_out;
 
@@ -190,7 +195,10 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
   da.alphabits = alpha_bits(dxt);
   da.dst = c.t565.as<uint32_t>();
   da.error = c.err.as<int>();
+  cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
+  if (tev && !cuda_ok(cudaEventRecord(tev[0], s), "cudaEventRecord")) return ST_CUDA_ERROR;
   if (!cuda_ok(launch_dither(da, opt.dither, c.scratch.as<uint8_t>(), s), "dither launch")) return ST_CUDA_ERROR;
+  if (tev && !cuda_ok(cudaEventRecord(tev[1], s), "cudaEventRecord")) return ST_CUDA_ERROR;
 
   EncodeArgs ea{};
   ea.t565 = c.t565.as<uint32_t>();
@@ -239,6 +247,10 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
       }
       if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
     }
+  }
+  if (tev) {
+    if (!cuda_ok(cudaEventRecord(tev[2], s), "cudaEventRecord")) return ST_CUDA_ERROR;
+    c.timed_calls++;
   }
   if (!cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord")) return ST_CUDA_ERROR;
   return ST_OK;
@@ -569,6 +581,42 @@ int s2tc_gpu_synchronize(void* stream) {
   if (!c.init()) return S2TC_ERR_CUDA;
   return check_error_flag(c, stream ? static_cast<cudaStream_t>(stream) : c.stream);
 }
+
+int s2tc_gpu_set_timing(int enable) {
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  if (enable && c.ev.empty()) {
+    c.ev.resize(3 * Context::kTimingSlots);
+    for (auto& e : c.ev)
+      if (!cuda_ok(cudaEventCreate(&e), "cudaEventCreate")) return S2TC_ERR_CUDA;
+  }
+  c.timing = enable != 0;
+  c.timed_calls = 0;
+  return S2TC_OK;
+}
+
+int s2tc_gpu_stage_ms(float* dither_ms, float* encode_ms, long long* calls) {
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  const long long n = std::min<long long>(c.timed_calls, Context::kTimingSlots);
+  double a = 0, b = 0;
+  for (long long i = 0; i < n; ++i) {
+    cudaEvent_t* e = &c.ev[3 * i];
+    float x = 0, y = 0;
+    if (!cuda_ok(cudaEventSynchronize(e[2]), "cudaEventSynchronize")) return S2TC_ERR_CUDA;
+    if (!cuda_ok(cudaEventElapsedTime(&x, e[0], e[1]), "cudaEventElapsedTime")) return S2TC_ERR_CUDA;
+    if (!cuda_ok(cudaEventElapsedTime(&y, e[1], e[2]), "cudaEventElapsedTime")) return S2TC_ERR_CUDA;
+    a += x;
+    b += y;
+  }
+  if (dither_ms) *dither_ms = float(a);
+  if (encode_ms) *encode_ms = float(b);
+  if (calls) *calls = n;
+  return S2TC_OK;
+}
+
+long long s2tc_gpu_kernel_launches(void) { return s2tc::launches_so_far(); }
 
 const char* s2tc_last_error(void) { return s2tc::g_last_error.c_str(); }
 

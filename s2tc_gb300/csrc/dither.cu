@@ -19,6 +19,7 @@
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "dither.h"
@@ -305,6 +306,7 @@ template <int SC>
 cudaError_t launch_simple(const DitherArgs& a, cudaStream_t s) {
   const long long npx = (long long)a.width * a.height;
   const unsigned grid = unsigned((npx + kTile - 1) / kTile);
+  count_launches(1);
   if (SC == 3) {
     k_dither_simple<SC, 0><<<grid, kThreads, 0, s>>>(a);
   } else if (a.alphabits == 1) {
@@ -317,7 +319,12 @@ cudaError_t launch_simple(const DitherArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+std::atomic<long long> g_launches{0};
+
 }  // namespace
+
+void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 size_t dither_scratch_bytes(long long npx) {
   const long long tiles = (npx + kTile - 1) / kTile;
@@ -332,6 +339,7 @@ cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream
   if (dither == DI_FLOYDSTEINBERG) return launch_dither_fs(a, scratch, s);
   if (dither == DI_NONE) {
     const unsigned grid = unsigned((npx + 255) / 256);
+    count_launches(1);
     if (a.srccomps == 3) k_dither_none<3><<<grid, 256, 0, s>>>(a);
     else k_dither_none<4><<<grid, 256, 0, s>>>(a);
     return cudaGetLastError();

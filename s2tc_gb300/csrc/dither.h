@@ -8,6 +8,10 @@
 
 namespace s2tc {
 
+// Kernels launched by this library since load (all translation units).
+void count_launches(int n);
+long long launches_so_far();
+
 struct DitherArgs {
   const uint8_t* src;  // packed RGB8/RGBA8, `width * srccomps` bytes per row
   int width, height, srccomps;

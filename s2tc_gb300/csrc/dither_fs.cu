@@ -257,6 +257,7 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const int abits = d.alphabits;
   // red/green/blue pass; for 3-component input the alpha byte is the constant
+  count_launches(1);
   if (d.srccomps == 3) {
     if (abits == 1) k_fs<3, 3, 1><<<nbands, kRows, 0, s>>>(a);
     else if (abits == 4) k_fs<3, 3, 15><<<nbands, kRows, 0, s>>>(a);
@@ -268,6 +269,7 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   if (abits == 8) {
     const long long npx = (long long)w * h;
+    count_launches(1);
     k_alpha_copy<<<unsigned((npx + 255) / 256), 256, 0, s>>>(d.src, a.dst, npx);
     return cudaGetLastError();
   }
@@ -280,6 +282,7 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
+  count_launches(1);
   if (abits == 1) k_fs<1, 4, 1><<<nbands, kRows, 0, s>>>(b);
   else k_fs<1, 4, 4><<<nbands, kRows, 0, s>>>(b);
   return cudaGetLastError();

@@ -10,6 +10,7 @@
 // DXT1/DXT3/DXT5 blocks, block rows `pitch` bytes apart.
 #include <cuda_runtime.h>
 
+#include "dither.h"
 #include "encode.h"
 #include "s2tc_device.cuh"
 
@@ -313,6 +314,7 @@ cudaError_t launch_r(const EncodeArgs& a, int refine, cudaStream_t s) {
   if (nb == 0) return cudaSuccess;
   const int threads = 128;
   const unsigned grid = unsigned((nb + threads - 1) / threads);
+  count_launches(1);
   switch (refine) {
     case RF_NEVER: k_encode<DXT, NORMAL, RF_NEVER><<<grid, threads, 0, s>>>(a); break;
     case RF_LOOP: k_encode<DXT, NORMAL, RF_LOOP><<<grid, threads, 0, s>>>(a); break;
