@@ -291,8 +291,11 @@ def main() -> None:
         sys.path.insert(0, str(ROOT / "oracle"))
         rng = np.random.default_rng(9)
         d_rand = torch.from_numpy(rng.integers(0, 2**31, nwords, dtype=np.int64).astype(np.uint32)).cuda()
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library treats a null stream as "use my own"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
+    assert sp != 0
 
     def step(i, rand=d_rand):
         s2.gpu_compress(sc, w, h, d_src[i % NIMG], fmt, d_dst[i % NIMG], opt=opt, d_rand=rand, stream=sp)
