@@ -124,6 +124,21 @@ int s2tc_gpu_stage_ms(float *dither_ms, float *encode_ms, long long *calls);
 /* Number of CUDA kernels this library has launched since it was loaded. */
 long long s2tc_gpu_kernel_launches(void);
 
+/* Compress one device-resident image without allocating any memory.  No
+ * counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (engines whose frame budget or memory pool forbids allocator
+ * calls).  Same arguments and bytes as s2tc_gpu_compress, but the scratch
+ * (dither state and 5:6:5 texel words) lives in one fixed device array of the
+ * library, held on every GPU that loads it until exit; images are limited to
+ * 4 Mi texels (S2TC_ERR_TOO_LARGE beyond), RANDOM_COLORS > 0 needs `d_rand`,
+ * and the call waits for `stream` before returning.  The first call on a
+ * device sets up the array's address: make it before any stream capture.
+ * Calls are serialised within the process; calls whose GPU work overlaps
+ * (e.g. from another library instance) race on the shared array. */
+int s2tc_gpu_compress_noalloc(int srccomps, int width, int height, const void *d_src, unsigned int destformat,
+			      void *d_dst, long long dst_pitch, const s2tc_options *opt, const unsigned int *d_rand,
+			      void *stream);
+
 /* Text of the last error this thread saw (empty when none). */
 const char *s2tc_last_error(void);
 

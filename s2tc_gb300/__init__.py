@@ -93,6 +93,9 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_gpu_compress.argtypes = [c_int, c_int, c_int, vp, c_uint, vp, c_ll,
                                       ctypes.POINTER(Options), vp, vp]
     lib.s2tc_gpu_compress.restype = c_int
+    lib.s2tc_gpu_compress_noalloc.argtypes = [c_int, c_int, c_int, vp, c_uint, vp, c_ll,
+                                              ctypes.POINTER(Options), vp, vp]
+    lib.s2tc_gpu_compress_noalloc.restype = c_int
     lib.s2tc_gpu_synchronize.argtypes = [vp]
     lib.s2tc_gpu_synchronize.restype = c_int
     lib.s2tc_rand_words.argtypes = [c_int, c_int, c_uint, ctypes.POINTER(Options)]
@@ -117,7 +120,7 @@ EXPORTED_SYMBOLS = (
     "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5", "rgb565_image",
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
     "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
-    "s2tc_gpu_kernel_launches",
+    "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc",
     "s2tc_last_error",
 )
 
@@ -247,6 +250,23 @@ def stage_ms() -> tuple[float, float, int]:
 
 def kernel_launches() -> int:
     return int(load().s2tc_gpu_kernel_launches())
+
+
+def gpu_compress_noalloc(srccomps: int, width: int, height: int, d_src, destformat: int, d_dst,
+                         dst_pitch: int | None = None, opt: Options | None = None, d_rand=None,
+                         stream: int | None = None) -> int:
+    """``s2tc_gpu_compress_noalloc``: like gpu_compress, but the library
+    allocates nothing (scratch in a fixed device array, images up to 4 Mi
+    texels; returns when done).  For callers that cannot allocate device
+    memory.  Returns the status code."""
+    if dst_pitch is None:
+        dst_pitch = ((width + 3) // 4) * block_bytes(destformat)
+    opt = opt if opt is not None else options_from_env()
+    src_p = d_src if isinstance(d_src, int) else _ptr(d_src)
+    dst_p = d_dst if isinstance(d_dst, int) else _ptr(d_dst)
+    rnd_p = None if d_rand is None else (d_rand if isinstance(d_rand, int) else _ptr(d_rand))
+    return int(load().s2tc_gpu_compress_noalloc(srccomps, width, height, src_p, destformat, dst_p, dst_pitch,
+                                                ctypes.byref(opt), rnd_p, stream))
 
 
 def gpu_synchronize(stream: int | None = None) -> None:
