@@ -23,15 +23,98 @@ namespace {
 
 constexpr int kMetric = S2TC_METRIC;
 
+using P = typename PrepT<kMetric>::T;
+
+// Slot (y*4+x) of input k of a full block: inputs are gathered x-outer,
+// y-inner (s2tc_algorithm.cpp:940-951).
+__device__ __forceinline__ constexpr int in_slot(int k) { return (k & 3) * 4 + (k >> 2); }
+
+// ------------------------------------------------------------------------
+// Full-block search without random candidates: 16 inputs, all 120 pairs,
+// distances held in registers (fully unrolled, compile-time indices).
+
+// reduce_colors_inplace (s2tc_algorithm.cpp:363-414) for n = m = 16.  Between
+// two inputs the reference evaluates dist(c[lo], c[hi]) once and uses it both
+// ways; pairs are visited in (i, j) lexicographic order and a pair is taken
+// when `bestsum < 0 || sum < bestsum`.
+__device__ __forceinline__ void reduce16_rgb(const P* tp, int& besti, int& bestj) {
+  int32_t D[16][16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 16; ++j) D[i][j] = pdist<kMetric>(tp[in_slot(i)], tp[in_slot(j)]);
+  int32_t bestsum = -1;
+  besti = 0;
+  bestj = 1;
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 16; ++j) {
+      int32_t sum = 0;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        if (k == i || k == j) continue;  // distance 0 to itself
+        const int32_t di = k < i ? D[k][i] : D[i][k];
+        const int32_t dj = k < j ? D[k][j] : D[j][k];
+        sum = wadd(sum, min(di, dj));
+      }
+      const bool take = bestsum < 0 || sum < bestsum;
+      bestsum = take ? sum : bestsum;
+      besti = take ? i : besti;
+      bestj = take ? j : bestj;
+    }
+}
+
+// reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) for n = m = 16
+// on the alpha values.  Each input's cost is the smallest squared distance to
+// the pair or to the fixed values 0 and 255; the minimum of squares of
+// non-negative numbers is the square of their minimum, so the search runs on
+// absolute differences.  Its conditional write-back into c[0]/c[1] reads the
+// candidates before changing them, so the result is simply the winning pair.
+__device__ __forceinline__ void reduce16_alpha(const int* ain, int& besti, int& bestj) {
+  int A[16][16];
+  int F[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) F[k] = min(ain[k], 255 - ain[k]);
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 16; ++j) A[i][j] = abs(ain[i] - ain[j]);
+  int32_t bestsum = -1;
+  besti = 0;
+  bestj = 1;
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 16; ++j) {
+      int32_t sum = 0;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        if (k == i || k == j) continue;
+        const int ai = k < i ? A[k][i] : A[i][k];
+        const int aj = k < j ? A[k][j] : A[j][k];
+        const int v = min(min(ai, aj), F[k]);
+        sum += v * v;
+      }
+      const bool take = bestsum < 0 || sum < bestsum;
+      bestsum = take ? sum : bestsum;
+      besti = take ? i : besti;
+      bestj = take ? j : bestj;
+    }
+}
+
+// ------------------------------------------------------------------------
+// General search: partial blocks, DXT1 blocks with transparent texels, and
+// random candidates.
+
 // Candidate c[j] of the pair search: the first n are the block's inputs in
 // x-outer, y-inner order; the rest are the random candidates of
 // s2tc_algorithm.cpp:962-993 drawn from the replayed rand() words.
 struct Candidates {
   C3 in[16];
+  P pin[16];
   int ain[16];
   int n;
-  // random candidates
-  int nr;
   const uint32_t* rnd;
   int stride;  // rand words per candidate: 3 (DXT1/DXT3) or 4 (DXT5)
   C3 lo;
@@ -51,39 +134,34 @@ __device__ __forceinline__ int cand_a(const Candidates& cs, int j) {
   return cs.alo + int(__ldg(r + 3) % uint32_t(cs.la));
 }
 
-// Distance of candidate row i to input k, with the reference's argument order:
-// between two inputs it is dist(c[min], c[max]) (s2tc_algorithm.cpp:375-383),
-// for a random candidate dist(c[i], c[k]) (:385-392).
-__device__ __forceinline__ int32_t in_dist(const Candidates& cs, int i, int k) {
-  if (i == k) return 0;
-  return i < k ? cdist<kMetric>(cs.in[i], cs.in[k]) : cdist<kMetric>(cs.in[k], cs.in[i]);
+// Distance row of candidate i against the inputs, with the reference's
+// argument order: between two inputs dist(c[min], c[max])
+// (s2tc_algorithm.cpp:375-383), for a random candidate dist(c[i], c[k])
+// (:385-392).  Entries k >= n are 0 and add nothing.
+__device__ __forceinline__ void dist_row(const Candidates& cs, int i, int32_t* row) {
+  if (i < cs.n) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      int32_t d = 0;
+      if (k < cs.n && k != i) d = i < k ? pdist<kMetric>(cs.pin[i], cs.pin[k]) : pdist<kMetric>(cs.pin[k], cs.pin[i]);
+      row[k] = d;
+    }
+  } else {
+    const P pi = prep<kMetric>(cand_rgb(cs, i));
+#pragma unroll
+    for (int k = 0; k < 16; ++k) row[k] = k < cs.n ? pdist<kMetric>(pi, cs.pin[k]) : 0;
+  }
 }
 
-// reduce_colors_inplace (s2tc_algorithm.cpp:363-414): first pair (i<j) in
-// lexicographic order that the reference's `bestsum < 0 || sum < bestsum`
-// rule keeps.  Sequential over pairs, so the rule is followed literally.
+// reduce_colors_inplace (s2tc_algorithm.cpp:363-414), sequential over pairs.
 __device__ void reduce_rgb(const Candidates& cs, int m, C3& c0, C3& c1) {
-  const int n = cs.n;
-  int32_t dm[16][16];
-  for (int i = 0; i < n; ++i)
-    for (int k = 0; k < n; ++k) dm[i][k] = in_dist(cs, i, k);
   int32_t bestsum = -1;
   int besti = 0, bestj = 1;
   int32_t ri[16], rj[16];
   for (int i = 0; i < m; ++i) {
-    if (i < n) {
-      for (int k = 0; k < 16; ++k) ri[k] = k < n ? dm[i][k] : 0;
-    } else {
-      C3 ci = cand_rgb(cs, i);
-      for (int k = 0; k < 16; ++k) ri[k] = k < n ? cdist<kMetric>(ci, cs.in[k]) : 0;
-    }
+    dist_row(cs, i, ri);
     for (int j = i + 1; j < m; ++j) {
-      if (j < n) {
-        for (int k = 0; k < 16; ++k) rj[k] = k < n ? dm[j][k] : 0;
-      } else {
-        C3 cj = cand_rgb(cs, j);
-        for (int k = 0; k < 16; ++k) rj[k] = k < n ? cdist<kMetric>(cj, cs.in[k]) : 0;
-      }
+      dist_row(cs, j, rj);
       int32_t sum = 0;
 #pragma unroll
       for (int k = 0; k < 16; ++k) sum = wadd(sum, min(ri[k], rj[k]));
@@ -99,16 +177,12 @@ __device__ void reduce_rgb(const Candidates& cs, int m, C3& c0, C3& c1) {
 }
 
 // reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) on the alpha
-// candidates.  Its conditional writes back into c[0]/c[1] read the candidates
-// before any of them changes, so the result is simply the winning pair.
+// candidates; see reduce16_alpha for why the result is the winning pair.
 __device__ void reduce_alpha(const Candidates& cs, int m, int& a0, int& a1) {
   const int n = cs.n;
-  int32_t fix[16];
+  int F[16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    int a = k < n ? cs.ain[k] : 0;
-    fix[k] = k < n ? min(a * a, (255 - a) * (255 - a)) : 0;
-  }
+  for (int k = 0; k < 16; ++k) F[k] = k < n ? min(cs.ain[k], 255 - cs.ain[k]) : 0;
   int32_t bestsum = -1;
   int besti = 0, bestj = 1;
   for (int i = 0; i < m; ++i) {
@@ -120,7 +194,8 @@ __device__ void reduce_alpha(const Candidates& cs, int m, int& a0, int& a1) {
       for (int k = 0; k < 16; ++k) {
         if (k < n) {
           const int ak = cs.ain[k];
-          sum = wadd(sum, min(min(adist(ai, ak), adist(aj, ak)), fix[k]));
+          const int v = min(min(abs(ai - ak), abs(aj - ak)), F[k]);
+          sum += v * v;
         }
       }
       if (bestsum < 0 || sum < bestsum) {
@@ -146,14 +221,17 @@ template <int DXT, bool NORMAL, int REFINE>
 __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* rnd, int prev_a1,
                             EncodedBlock& out) {
   constexpr bool TRANS = DXT == DXT1;
+  P tp[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) tp[i] = prep<kMetric>(texel_c3(bt.px[i]));
   C3 c0, c1;
   int a0 = 0, a1 = 0;
   if (!NORMAL) {
     // darkest / brightest by distance to black (:879-935)
-    const C3 black{0, 0, 0};
+    const P black = prep<kMetric>(C3{0, 0, 0});
     int32_t dmin = 0x7FFFFFFF, dmax = 0;
     c0 = C3{31, 63, 31};
-    c1 = black;
+    c1 = C3{0, 0, 0};
     if (DXT == DXT5) a0 = a1 = texel_a(bt.px[0]);
 #pragma unroll
     for (int x = 0; x < 4; ++x)
@@ -162,10 +240,9 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
         if (x >= bt.w || y >= bt.h) continue;
         uint32_t t = bt.px[y * 4 + x];
         if (DXT == DXT1 && (t >> 24) == 0) continue;
-        C3 c = texel_c3(t);
-        int32_t d = cdist<kMetric>(c, black);
-        if (d > dmax) { dmax = d; c1 = c; }
-        if (d < dmin) { dmin = d; c0 = c; }
+        int32_t d = pdist<kMetric>(tp[y * 4 + x], black);
+        if (d > dmax) { dmax = d; c1 = texel_c3(t); }
+        if (d < dmin) { dmin = d; c0 = texel_c3(t); }
         if (DXT == DXT5) {
           int a = texel_a(t);
           if (a != 255) {
@@ -175,51 +252,72 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
         }
       }
   } else {
-    Candidates cs;
-    cs.n = 0;
+    bool full = bt.w == 4 && bt.h == 4 && nrandom <= 0;
+    if (DXT == DXT1 && full) {
 #pragma unroll
-    for (int x = 0; x < 4; ++x)
+      for (int i = 0; i < 16; ++i) full = full && (bt.px[i] >> 24) != 0;
+    }
+    if (full) {
+      int bi, bj;
+      reduce16_rgb(tp, bi, bj);
+      c0 = texel_c3(bt.px[(bi & 3) * 4 + (bi >> 2)]);
+      c1 = texel_c3(bt.px[(bj & 3) * 4 + (bj >> 2)]);
+      if (DXT == DXT5) {
+        int ain[16];
 #pragma unroll
-      for (int y = 0; y < 4; ++y) {
-        if (x >= bt.w || y >= bt.h) continue;
-        uint32_t t = bt.px[y * 4 + x];
-        if (DXT == DXT1 && (t >> 24) == 0) continue;
-        cs.in[cs.n] = texel_c3(t);
-        cs.ain[cs.n] = texel_a(t);
-        cs.n++;
+        for (int k = 0; k < 16; ++k) ain[k] = texel_a(bt.px[in_slot(k)]);
+        reduce16_alpha(ain, bi, bj);
+        a0 = texel_a(bt.px[(bi & 3) * 4 + (bi >> 2)]);
+        a1 = texel_a(bt.px[(bj & 3) * 4 + (bj >> 2)]);
       }
-    if (cs.n == 0) {
-      cs.n = 1;
-      cs.in[0] = C3{0, 0, 0};
-      cs.ain[0] = 0;
-    }
-    int m = cs.n;
-    cs.nr = 0;
-    cs.rnd = rnd;
-    cs.stride = DXT == DXT5 ? 4 : 3;
-    if (nrandom > 0) {
-      C3 lo = cs.in[0], hi = cs.in[0];
-      int alo = DXT == DXT5 ? cs.ain[0] : 0, ahi = alo;
-      for (int k = 1; k < cs.n; ++k) {
-        lo.r = min(lo.r, cs.in[k].r); lo.g = min(lo.g, cs.in[k].g); lo.b = min(lo.b, cs.in[k].b);
-        hi.r = max(hi.r, cs.in[k].r); hi.g = max(hi.g, cs.in[k].g); hi.b = max(hi.b, cs.in[k].b);
-        if (DXT == DXT5) { alo = min(alo, cs.ain[k]); ahi = max(ahi, cs.ain[k]); }
+    } else {
+      Candidates cs;
+      cs.n = 0;
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+          if (x >= bt.w || y >= bt.h) continue;
+          uint32_t t = bt.px[y * 4 + x];
+          if (DXT == DXT1 && (t >> 24) == 0) continue;
+          cs.in[cs.n] = texel_c3(t);
+          cs.pin[cs.n] = tp[y * 4 + x];
+          cs.ain[cs.n] = texel_a(t);
+          cs.n++;
+        }
+      if (cs.n == 0) {
+        cs.n = 1;
+        cs.in[0] = C3{0, 0, 0};
+        cs.pin[0] = prep<kMetric>(cs.in[0]);
+        cs.ain[0] = 0;
       }
-      cs.lo = lo;
-      cs.lr = hi.r - lo.r + 1; cs.lg = hi.g - lo.g + 1; cs.lb = hi.b - lo.b + 1;
-      cs.alo = alo; cs.la = ahi - alo + 1;
-      cs.nr = nrandom;
-      m = cs.n + nrandom;
-    } else if (cs.n == 1) {
-      // single input (:996-1001): the colour is duplicated; the reference's
-      // second alpha candidate is whatever the previous block left in that slot
-      cs.in[1] = cs.in[0];
-      cs.ain[1] = prev_a1 >= 0 ? prev_a1 : cs.ain[0];
-      cs.n = 2;
-      m = 2;
+      int m = cs.n;
+      cs.rnd = rnd;
+      cs.stride = DXT == DXT5 ? 4 : 3;
+      if (nrandom > 0) {
+        C3 lo = cs.in[0], hi = cs.in[0];
+        int alo = DXT == DXT5 ? cs.ain[0] : 0, ahi = alo;
+        for (int k = 1; k < cs.n; ++k) {
+          lo.r = min(lo.r, cs.in[k].r); lo.g = min(lo.g, cs.in[k].g); lo.b = min(lo.b, cs.in[k].b);
+          hi.r = max(hi.r, cs.in[k].r); hi.g = max(hi.g, cs.in[k].g); hi.b = max(hi.b, cs.in[k].b);
+          if (DXT == DXT5) { alo = min(alo, cs.ain[k]); ahi = max(ahi, cs.ain[k]); }
+        }
+        cs.lo = lo;
+        cs.lr = hi.r - lo.r + 1; cs.lg = hi.g - lo.g + 1; cs.lb = hi.b - lo.b + 1;
+        cs.alo = alo; cs.la = ahi - alo + 1;
+        m = cs.n + nrandom;
+      } else if (cs.n == 1) {
+        // single input (:996-1001): the colour is duplicated; the reference's
+        // second alpha candidate is whatever the previous block left in that slot
+        cs.in[1] = cs.in[0];
+        cs.pin[1] = cs.pin[0];
+        cs.ain[1] = prev_a1 >= 0 ? prev_a1 : cs.ain[0];
+        cs.n = 2;
+        m = 2;
+      }
+      reduce_rgb(cs, m, c0, c1);
+      if (DXT == DXT5) reduce_alpha(cs, m, a0, a1);
     }
-    reduce_rgb(cs, m, c0, c1);
-    if (DXT == DXT5) reduce_alpha(cs, m, a0, a1);
   }
 
   // equal endpoints are bumped apart (:1009-1027)
@@ -228,7 +326,7 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
     if (a0 == 255) --a1; else ++a1;
   }
 
-  uint32_t cbits = colour_refine<kMetric, TRANS, REFINE>(bt, c0, c1);
+  uint32_t cbits = colour_refine<kMetric, TRANS, REFINE>(bt, tp, c0, c1);
   const uint64_t colour = uint64_t(pack565(c0)) | (uint64_t(pack565(c1)) << 16) | (uint64_t(cbits) << 32);
   int leftover = a1;
   if (DXT == DXT1) {

@@ -80,39 +80,70 @@ __device__ __forceinline__ int32_t nm_dist(NUnit a, NUnit b) {
   return __float2int_rz(__fmul_rn(100000.0f, s));
 }
 
+// Each metric is evaluated on a per-colour "prepared" form computed once per
+// colour: the squared components for SRGB, (Y, U, V) with the square-rooted
+// luma for SRGB_MIXED, the unit vector for NORMALMAP, the plain components
+// otherwise.  pdist(prep(a), prep(b)) equals the reference's dist(a, b)
+// operation for operation.
 template <int METRIC>
-__device__ __forceinline__ int32_t cdist(C3 a, C3 b) {
-  if (METRIC == CD_AVG) {
+struct PrepT {
+  using T = C3;
+};
+template <>
+struct PrepT<CD_NORMALMAP> {
+  using T = NUnit;
+};
+
+template <int METRIC>
+__device__ __forceinline__ typename PrepT<METRIC>::T prep(C3 c) {
+  if constexpr (METRIC == CD_SRGB) {
+    return C3{c.r * c.r, c.g * c.g, c.b * c.b};
+  } else if constexpr (METRIC == CD_SRGB_MIXED) {
+    const int y = srgb_luma(c.r, c.g, c.b);
+    return C3{y, c.r * 191 - y, c.b * 191 - y};
+  } else if constexpr (METRIC == CD_NORMALMAP) {
+    return nm_unit(c);
+  } else {
+    return c;
+  }
+}
+
+template <int METRIC>
+__device__ __forceinline__ int32_t pdist(const typename PrepT<METRIC>::T& a, const typename PrepT<METRIC>::T& b) {
+  if constexpr (METRIC == CD_NORMALMAP) {
+    return nm_dist(a, b);
+  } else if constexpr (METRIC == CD_AVG) {
     int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
     return ((dr * dr) << 2) + dg * dg + ((db * db) << 2);
-  } else if (METRIC == CD_W0AVG) {
+  } else if constexpr (METRIC == CD_W0AVG) {
     int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
     return dr * dr + dg * dg + db * db;
-  } else if (METRIC == CD_WAVG) {
+  } else if constexpr (METRIC == CD_WAVG) {
     int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
     return ((dr * dr) << 2) + ((dg * dg) << 2) + db * db;
-  } else if (METRIC == CD_YUV || METRIC == CD_RGB) {
+  } else if constexpr (METRIC == CD_YUV || METRIC == CD_RGB) {
     int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
     int y = METRIC == CD_YUV ? dr * 60 + dg * 59 + db * 22 : dr * 42 + dg * 72 + db * 14;
     int u = dr * 202 - y, v = db * 202 - y;
     return wadd(wadd(wmul(y, y) << 1, shrr<3>(wmul(u, u))), shrr<4>(wmul(v, v)));
-  } else if (METRIC == CD_SRGB) {
-    int dr = a.r * a.r - b.r * b.r, dg = a.g * a.g - b.g * b.g, db = a.b * a.b - b.b * b.b;
+  } else if constexpr (METRIC == CD_SRGB) {
+    // components are already squared
+    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
     int y = dr * 84 + dg * 72 + db * 28;
     int u = dr * 409 - y, v = db * 409 - y;
     int32_t sy = wmul(shrr<3>(y), shrr<4>(y));
     int32_t su = wmul(shrr<3>(u), shrr<4>(u));
     int32_t sv = wmul(shrr<3>(v), shrr<4>(v));
     return wadd(wadd(shrr<4>(sy), shrr<8>(su)), shrr<9>(sv));
-  } else if (METRIC == CD_SRGB_MIXED) {
-    int ay = srgb_luma(a.r, a.g, a.b), by = srgb_luma(b.r, b.g, b.b);
-    int y = ay - by;
-    int u = (a.r * 191 - ay) - (b.r * 191 - by);
-    int v = (a.b * 191 - ay) - (b.b * 191 - by);
+  } else {  // CD_SRGB_MIXED: (Y, U, V)
+    int y = a.r - b.r, u = a.g - b.g, v = a.b - b.b;
     return wadd(wadd(wmul(y, y) << 3, shrr<1>(wmul(u, u))), shrr<2>(wmul(v, v)));
-  } else {  // CD_NORMALMAP
-    return nm_dist(nm_unit(a), nm_unit(b));
   }
+}
+
+template <int METRIC>
+__device__ __forceinline__ int32_t cdist(C3 a, C3 b) {
+  return pdist<METRIC>(prep<METRIC>(a), prep<METRIC>(b));
 }
 
 __device__ __forceinline__ int32_t adist(int a, int b) { return (a - b) * (a - b); }
@@ -135,15 +166,17 @@ struct ColourAcc {
 };
 
 // s2tc_algorithm.cpp:582-643 (colour, two references): nearest endpoint per
-// texel, ties to endpoint 0; DXT1 alpha-0 texels take index 3.  Visits x-outer,
-// y-inner like the reference; the order matters only for the score sum, which
-// is order-independent, so any order gives the same result.
+// texel, ties to endpoint 0; DXT1 alpha-0 texels take index 3.  `tp` holds the
+// block's texels in prepared form (slot y*4+x).  The reference visits texels
+// x-outer, y-inner; the results (per-texel indices, sums) do not depend on
+// the order.
 template <int METRIC, bool TRANS, bool ACC>
-__device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, C3 r0, C3 r1, uint32_t& bits,
-                                                ColourAcc& acc) {
+__device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, const typename PrepT<METRIC>::T* tp, C3 r0,
+                                                C3 r1, uint32_t& bits, ColourAcc& acc) {
   uint32_t score = 0;
   bits = 0;
   if (ACC) acc = ColourAcc{0, 0, 0, 0, 0, 0, 0, 0};
+  const auto p0 = prep<METRIC>(r0), p1 = prep<METRIC>(r1);
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
     const int x = i & 3, y = i >> 2;
@@ -153,10 +186,10 @@ __device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, C3 r0, C3
       bits |= 3u << (2 * i);
       continue;
     }
-    C3 c = texel_c3(t);
-    int32_t d0 = cdist<METRIC>(c, r0), d1 = cdist<METRIC>(c, r1);
+    int32_t d0 = pdist<METRIC>(tp[i], p0), d1 = pdist<METRIC>(tp[i], p1);
     const bool one = d1 < d0;
     if (ACC) {
+      C3 c = texel_c3(t);
       if (one) {
         acc.n1++;
         acc.s1r += c.r; acc.s1g += c.g; acc.s1b += c.b;
@@ -200,14 +233,15 @@ __device__ __forceinline__ void colour_finish(uint32_t& bits, C3& c0, C3& c1) {
 
 // Colour refinement NEVER / ALWAYS / LOOP (s2tc_algorithm.cpp:767-860).
 template <int METRIC, bool TRANS, int REFINE>
-__device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, C3& c0, C3& c1) {
+__device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, const typename PrepT<METRIC>::T* tp, C3& c0,
+                                                  C3& c1) {
   uint32_t bits;
   ColourAcc acc;
   if (REFINE == RF_NEVER) {
     if (TRANS ? c3_lt(c1, c0) : c3_lt(c0, c1)) {
       C3 t = c0; c0 = c1; c1 = t;
     }
-    colour_pass<METRIC, TRANS, false>(bt, c0, c1, bits, acc);
+    colour_pass<METRIC, TRANS, false>(bt, tp, c0, c1, bits, acc);
     return bits;
   } else if (REFINE == RF_LOOP) {
     C3 n0 = c0, n1 = c1;
@@ -215,7 +249,7 @@ __device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, C3& c0,
     bits = 0;
     for (;;) {
       uint32_t b2;
-      uint32_t s2 = colour_pass<METRIC, TRANS, true>(bt, n0, n1, b2, acc);
+      uint32_t s2 = colour_pass<METRIC, TRANS, true>(bt, tp, n0, n1, b2, acc);
       if (!(s2 < best)) break;
       bits = b2;
       best = s2;
@@ -224,7 +258,7 @@ __device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, C3& c0,
       if (!colour_means(acc, n0, n1)) break;
     }
   } else {
-    colour_pass<METRIC, TRANS, true>(bt, c0, c1, bits, acc);
+    colour_pass<METRIC, TRANS, true>(bt, tp, c0, c1, bits, acc);
     colour_means(acc, c0, c1);
   }
   colour_finish<TRANS>(bits, c0, c1);
