@@ -56,11 +56,17 @@ def _stale(obj: Path, deps) -> bool:
 def build_library(verbose: bool = False, force: bool = False) -> Path:
     nvcc = _nvcc()
     OBJ_DIR.mkdir(parents=True, exist_ok=True)
+    # extra nvcc flags (e.g. -D tuning macros) force a rebuild when they change
+    extra = os.environ.get("S2TC_NVCC_EXTRA", "").split()
+    stamp = OBJ_DIR / "flags.txt"
+    if not stamp.exists() or stamp.read_text() != " ".join(extra):
+        force = True
+        stamp.write_text(" ".join(extra))
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "s2tc_gb300.h"]
     jobs = []
-    for src, obj, extra in _units():
+    for src, obj, unit_flags in _units():
         if force or _stale(obj, [src, *headers]):
-            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *unit_flags, *extra, "-c", str(src), "-o", str(obj)]
             jobs.append(cmd)
     if jobs:
         workers = max(1, min(len(jobs), os.cpu_count() or 4))

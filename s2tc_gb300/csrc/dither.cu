@@ -7,10 +7,14 @@
 //   - a channel's carried error takes few values (red/blue: -7..7, green:
 //     -3..3, 4-bit alpha: -15..15), so the effect of a run of texels on it is a
 //     small table state -> state; tables compose;
-//   - each thread builds the table of its 16-texel segment, the CTA composes
+//   - each thread builds the table of its 64-texel segment, the CTA composes
 //     them (Hillis-Steele in shared memory), tiles chain their aggregates with
 //     a decoupled look-back, and every thread then replays its segment from
 //     its exact start state;
+//   - the 5- and 6-bit channels run all start states at once, four per 32-bit
+//     word (one byte each): one texel step is then a handful of byte-parallel
+//     adds and masks driven by constants that depend only on the source byte
+//     (see swar_step);
 //   - the 1-bit alpha chain (diffuse1) is a rotation: its carried error after
 //     k texels is ((sum of sources + 127) mod 255) - 127, so its "table" is a
 //     sum mod 255.
@@ -28,7 +32,7 @@ namespace s2tc {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSeg = 16;
+constexpr int kSeg = 64;  // texels per thread, contiguous in raster order
 constexpr int kTile = kThreads * kSeg;
 
 // Table layout (bytes) inside one 72-byte record: red 15 states at 0, green 7
@@ -116,50 +120,47 @@ __device__ __forceinline__ void identity(uint8_t* t) {
   if (AK == 1) t[kOffA] = 0;
 }
 
-// Load the thread's segment (texels [p0, p0 + nvalid)) as RGBA words; for
-// 3-component input the alpha byte is left 0.
-template <int SC>
-__device__ __forceinline__ void load_seg(const uint8_t* __restrict__ src, long long p0, int nvalid, uint32_t* px) {
-  const uint8_t* s = src + p0 * SC;
-  const bool vec = nvalid == kSeg && (reinterpret_cast<uintptr_t>(s) & 15) == 0;
-  if (SC == 4) {
-    if (vec) {
-      const uint4* v = reinterpret_cast<const uint4*>(s);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        uint4 w = __ldg(v + q);
-        px[4 * q + 0] = w.x; px[4 * q + 1] = w.y; px[4 * q + 2] = w.z; px[4 * q + 3] = w.w;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < kSeg; ++k)
-        px[k] = k < nvalid ? (uint32_t(s[4 * k]) | (uint32_t(s[4 * k + 1]) << 8) | (uint32_t(s[4 * k + 2]) << 16) |
-                              (uint32_t(s[4 * k + 3]) << 24))
-                           : 0u;
-    }
-  } else {
-    if (vec) {
-      uint32_t w[12];
-      const uint4* v = reinterpret_cast<const uint4*>(s);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        uint4 t = __ldg(v + q);
-        w[4 * q + 0] = t.x; w[4 * q + 1] = t.y; w[4 * q + 2] = t.z; w[4 * q + 3] = t.w;
-      }
-#pragma unroll
-      for (int k = 0; k < kSeg; ++k) {
-        // texel k occupies bytes 3k..3k+2 of the 48-byte segment
-        const int b0 = 3 * k;
-        uint64_t pair = uint64_t(w[b0 >> 2]) | (uint64_t(w[min((b0 >> 2) + 1, 11)]) << 32);
-        px[k] = uint32_t(pair >> (8 * (b0 & 3))) & 0xFFFFFFu;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < kSeg; ++k)
-        px[k] = k < nvalid ? (uint32_t(s[3 * k]) | (uint32_t(s[3 * k + 1]) << 8) | (uint32_t(s[3 * k + 2]) << 16))
-                           : 0u;
-    }
-  }
+// ---------------------------------------------------------------- SWAR step
+// For a channel quantised with shift k (k = 3: 5 bits, k = 2: 6 bits) let
+// E = 2^k - 1 be the largest carried error, e = d + E in [0, 2E] the state and
+// src = 2^k q + r.  With t = r + e and s = src + d = 2^k q + t - E, qstep gives
+//   e' = ((t + 1) mod 2^k) + E - base - [t >= T]           (0 <= s <= 255)
+// where base = (2^k q - E) >> (8 - k) and T = 2^(8-k) (base + 1) - (2^k q - E)
+// (the window of t values is narrower than 2^(8-k), so s >> (8 - k) takes at
+// most two values), e' = t when s < 0 (q = 0, t < E) and e' = t - E when
+// s > 255 (q = maxv, t > 2E).  Both clamps are the middle formula plus or
+// minus 2^k + 1, selected by [t >= T].  Every byte of a word holds one state
+// biased by 16, so no lane ever borrows from its neighbour, and one step is
+//   t = ub + rm; m = (t + 1) & E; g = ((t + 128 - T) >> 7) & 1; ub' = g*j1 + m + bc
+// with per-source-byte constants rm, kk = 128 - T, bc, j1 (SwarConst).
+
+struct SwarConst {
+  uint32_t rm, kk, bc, j1;
+};
+
+template <int K>
+__device__ __forceinline__ uint4 swar_const(int src) {
+  constexpr int E = (1 << K) - 1, maxv = 255 >> K;
+  const int r = src & E, q = src >> K;
+  const int base = ((1 << K) * q - E) >> (8 - K);
+  const int T = (1 << (8 - K)) * (base + 1) - ((1 << K) * q - E);
+  const int L = q == 0 ? (1 << K) + 1 : 0, H = q == maxv ? (1 << K) + 1 : 0;
+  return make_uint4(uint32_t(r) * 0x01010101u - 0x10101010u, uint32_t(128 - T) * 0x01010101u,
+                    uint32_t(16 + E - base - L) * 0x01010101u, uint32_t(H + L - 1));
+}
+
+template <int K>
+__device__ __forceinline__ uint32_t swar_step(uint32_t ub, const uint4& c) {
+  constexpr uint32_t MASK = uint32_t((1 << K) - 1) * 0x01010101u;
+  const uint32_t t = ub + c.x;
+  const uint32_t m = (t + 0x01010101u) & MASK;
+  const uint32_t g = ((t + c.y) >> 7) & 0x01010101u;
+  return g * c.w + (m + c.z);
+}
+
+// Unpack SWAR words (states biased by 16) into a byte table.
+__device__ __forceinline__ void swar_store(const uint32_t* w, int nstates, uint8_t* out) {
+  for (int s = 0; s < nstates; ++s) out[s] = uint8_t(((w[s >> 2] >> (8 * (s & 3))) & 0xFF) - 16);
 }
 
 using Status = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
@@ -167,13 +168,52 @@ constexpr unsigned long long kAggReady = 1ull << 32;
 constexpr unsigned long long kIncReady = 2ull << 32;
 constexpr int kSpinLimit = 1 << 22;
 
+// Texel k (0..3) of a group of four, as an RGBA word, from raw words `w`
+// (four texels = 16 bytes for RGBA, 12 bytes for RGB).
+template <int SC>
+__device__ __forceinline__ uint32_t texel_of(const uint32_t* w, int k) {
+  if (SC == 4) return w[k];
+  const int b0 = 3 * k;
+  const uint64_t pair = uint64_t(w[b0 >> 2]) | (uint64_t(w[min((b0 >> 2) + 1, 2)]) << 32);
+  return uint32_t(pair >> (8 * (b0 & 3))) & 0xFFFFFFu;
+}
+
+// Four texels [p, p + 4) of the image as RGBA words (alpha 0 for RGB input);
+// texels at or beyond npx read as 0 and must not be used.
+template <int SC>
+__device__ __forceinline__ void load4(const uint8_t* __restrict__ src, long long p, long long npx, uint32_t* px) {
+  const uint8_t* s = src + p * SC;
+  if (p + 4 <= npx && (reinterpret_cast<uintptr_t>(s) & 3) == 0) {
+    uint32_t w[4];
+    const uint32_t* v = reinterpret_cast<const uint32_t*>(s);
+#pragma unroll
+    for (int i = 0; i < SC; ++i) w[i] = __ldg(v + i);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) px[k] = texel_of<SC>(w, k);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      uint32_t v = 0;
+      if (p + k < npx) {
+        const uint8_t* t = s + k * SC;
+        v = uint32_t(t[0]) | (uint32_t(t[1]) << 8) | (uint32_t(t[2]) << 16);
+        if (SC == 4) v |= uint32_t(t[3]) << 24;
+      }
+      px[k] = v;
+    }
+  }
+}
+
 template <int SC, int AK>
 __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
   __shared__ __align__(16) uint8_t tbl[2][kThreads][kRec];
+  __shared__ uint4 s_c3[256], s_c2[256];
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_carry;
 
   const int t = threadIdx.x;
+  s_c3[t] = swar_const<3>(t);
+  s_c2[t] = swar_const<2>(t);
   if (t == 0) s_tile = atomicAdd(a.ticket, 1u);
   __syncthreads();
   const long long tile = s_tile;
@@ -181,22 +221,46 @@ __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
   const long long p0 = tile * kTile + (long long)t * kSeg;
   const int nvalid = int(max(0ll, min((long long)kSeg, npx - p0)));
 
-  uint32_t px[kSeg];
-  load_seg<SC>(a.src, p0, nvalid, px);
-
-  // segment tables
+  // segment tables: all start states at once, four per word
+  uint32_t wr[4] = {0x13121110u, 0x17161514u, 0x1B1A1918u, 0x171E1D1Cu};  // red states 0..14 (+pad)
+  uint32_t wb[4] = {0x13121110u, 0x17161514u, 0x1B1A1918u, 0x171E1D1Cu};  // blue
+  uint32_t wg[2] = {0x13121110u, 0x13161514u};                            // green states 0..6 (+pad)
+  int asum = 0;
   uint8_t* mine = tbl[0][t];
-  seg_table<3>(px, nvalid, 0, mine + kOffR);
-  seg_table<2>(px, nvalid, 1, mine + kOffG);
-  seg_table<3>(px, nvalid, 2, mine + kOffB);
-  if (AK == 4) seg_table<4>(px, nvalid, 3, mine + kOffA);
-  if (AK == 1) {
-    int sum = 0;
-#pragma unroll
-    for (int k = 0; k < kSeg; ++k)
-      if (k < nvalid) sum += chan_of(px[k], 3);
-    mine[kOffA] = uint8_t(sum % 255);
+  if (AK == 4) {
+    for (int s = 0; s < QChan<4>::kStates; ++s) mine[kOffA + s] = uint8_t(s);
   }
+  for (int k0 = 0; k0 < nvalid; k0 += 4) {
+    uint32_t px[4];
+    load4<SC>(a.src, p0 + k0, npx, px);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (k0 + k < nvalid) {
+        const uint32_t p = px[k];
+        const uint4 cr = s_c3[p & 0xFF], cg = s_c2[(p >> 8) & 0xFF], cb = s_c3[(p >> 16) & 0xFF];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) wr[i] = swar_step<3>(wr[i], cr);
+#pragma unroll
+        for (int i = 0; i < 2; ++i) wg[i] = swar_step<2>(wg[i], cg);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) wb[i] = swar_step<3>(wb[i], cb);
+        if (AK == 1) asum += int(p >> 24);
+        if (AK == 4) {
+          // 4-bit alpha: 31 states, stepped one by one
+          const int src = int(p >> 24);
+          for (int s = 0; s < QChan<4>::kStates; ++s) {
+            int d = int(mine[kOffA + s]) - QChan<4>::kOff;
+            qstep<4>(d, src);
+            mine[kOffA + s] = uint8_t(d + QChan<4>::kOff);
+          }
+        }
+      }
+    }
+  }
+  swar_store(wr, QChan<3>::kStates, mine + kOffR);
+  swar_store(wg, QChan<2>::kStates, mine + kOffG);
+  swar_store(wb, QChan<3>::kStates, mine + kOffB);
+  if (AK == 1) mine[kOffA] = uint8_t(asum % 255);
   __syncthreads();
 
   // inclusive scan of the tables across the CTA
@@ -254,39 +318,40 @@ __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
   __syncthreads();
 
   // replay the segment from its exact start state
-  uint32_t start = t == 0 ? s_carry : apply<AK>(tbl[cur][t - 1], s_carry);
+  const uint32_t start = t == 0 ? s_carry : apply<AK>(tbl[cur][t - 1], s_carry);
   int dr = int(start & 0xFF) - QChan<3>::kOff;
   int dg = int((start >> 8) & 0xFF) - QChan<2>::kOff;
   int db = int((start >> 16) & 0xFF) - QChan<3>::kOff;
   int da = AK == 4 ? int(start >> 24) - QChan<4>::kOff : int(start >> 24) - 127;
-  uint32_t out[kSeg];
-#pragma unroll
-  for (int k = 0; k < kSeg; ++k) {
-    const uint32_t p = px[k];
-    uint32_t q = uint32_t(qstep<3>(dr, chan_of(p, 0))) | (uint32_t(qstep<2>(dg, chan_of(p, 1))) << 8) |
-                 (uint32_t(qstep<3>(db, chan_of(p, 2))) << 16);
-    uint32_t qa;
-    if (AK == 4) {
-      qa = uint32_t(qstep<4>(da, chan_of(p, 3)));
-    } else if (AK == 1) {
-      // diffuse1 (s2tc_algorithm.cpp:1208-1216)
-      const int v = chan_of(p, 3) + da;
-      qa = v >= 128;
-      da = v - (qa ? 255 : 0);
-    } else if (AK == 8) {
-      qa = uint32_t(chan_of(p, 3));
-    } else {
-      qa = uint32_t(a.alpha_const);
-    }
-    out[k] = q | (qa << 24);
-  }
   uint32_t* o = a.dst + p0;
-  if (nvalid == kSeg) {
-    uint4* v = reinterpret_cast<uint4*>(o);
+  for (int k0 = 0; k0 < nvalid; k0 += 4) {
+    uint32_t px[4], out[4];
+    load4<SC>(a.src, p0 + k0, npx, px);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = make_uint4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
-  } else {
-    for (int k = 0; k < nvalid; ++k) o[k] = out[k];
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t p = px[k];
+      uint32_t q = uint32_t(qstep<3>(dr, chan_of(p, 0))) | (uint32_t(qstep<2>(dg, chan_of(p, 1))) << 8) |
+                   (uint32_t(qstep<3>(db, chan_of(p, 2))) << 16);
+      uint32_t qa;
+      if (AK == 4) {
+        qa = uint32_t(qstep<4>(da, chan_of(p, 3)));
+      } else if (AK == 1) {
+        // diffuse1 (s2tc_algorithm.cpp:1208-1216)
+        const int v = chan_of(p, 3) + da;
+        qa = v >= 128;
+        da = v - (qa ? 255 : 0);
+      } else if (AK == 8) {
+        qa = uint32_t(chan_of(p, 3));
+      } else {
+        qa = uint32_t(a.alpha_const);
+      }
+      out[k] = q | (qa << 24);
+    }
+    if (k0 + 4 <= nvalid) {
+      *reinterpret_cast<uint4*>(o + k0) = make_uint4(out[0], out[1], out[2], out[3]);
+    } else {
+      for (int k = 0; k < nvalid - k0; ++k) o[k0 + k] = out[k];
+    }
   }
 }
 

@@ -30,39 +30,70 @@ using P = typename PrepT<kMetric>::T;
 __device__ __forceinline__ constexpr int in_slot(int k) { return (k & 3) * 4 + (k >> 2); }
 
 // ------------------------------------------------------------------------
-// Full-block search without random candidates: 16 inputs, all 120 pairs,
-// distances held in registers (fully unrolled, compile-time indices).
+// Full-block search without random candidates: 16 inputs, all 120 pairs.
+// The loop runs over the inputs k; the 120 pair sums stay in registers and
+// every iteration adds min(d(i,k), d(j,k)) to each of them, so the loop body is
+// small (a few hundred instructions) while every index into the sums is a
+// compile-time constant.  Input k's prepared colour comes from a per-thread
+// column in shared memory.
 
-// reduce_colors_inplace (s2tc_algorithm.cpp:363-414) for n = m = 16.  Between
-// two inputs the reference evaluates dist(c[lo], c[hi]) once and uses it both
-// ways; pairs are visited in (i, j) lexicographic order and a pair is taken
-// when `bestsum < 0 || sum < bestsum`.
-__device__ __forceinline__ void reduce16_rgb(const P* tp, int& besti, int& bestj) {
-  int32_t D[16][16];
-#pragma unroll
-  for (int i = 0; i < 16; ++i)
-#pragma unroll
-    for (int j = i + 1; j < 16; ++j) D[i][j] = pdist<kMetric>(tp[in_slot(i)], tp[in_slot(j)]);
+constexpr int kThreadsPerCta = 128;
+
+// The metrics other than SRGB are symmetric in their arguments.
+constexpr bool kSymmetric = kMetric != CD_SRGB;
+
+// Per-thread scratch columns in shared memory (index [k][thread]).
+struct Scratch16 {
+  P pin[16][kThreadsPerCta];
+  int ain[16][kThreadsPerCta];
+};
+
+// Pick the pair the reference keeps: pairs in (i, j) lexicographic order,
+// taken when `bestsum < 0 || sum < bestsum` (s2tc_algorithm.cpp:404-409).
+__device__ __forceinline__ void pick_pair(const int32_t* S, int& besti, int& bestj) {
   int32_t bestsum = -1;
   besti = 0;
   bestj = 1;
+  int p = 0;
 #pragma unroll
   for (int i = 0; i < 16; ++i)
 #pragma unroll
-    for (int j = i + 1; j < 16; ++j) {
-      int32_t sum = 0;
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        if (k == i || k == j) continue;  // distance 0 to itself
-        const int32_t di = k < i ? D[k][i] : D[i][k];
-        const int32_t dj = k < j ? D[k][j] : D[j][k];
-        sum = wadd(sum, min(di, dj));
-      }
-      const bool take = bestsum < 0 || sum < bestsum;
-      bestsum = take ? sum : bestsum;
+    for (int j = i + 1; j < 16; ++j, ++p) {
+      const bool take = bestsum < 0 || S[p] < bestsum;
+      bestsum = take ? S[p] : bestsum;
       besti = take ? i : besti;
       bestj = take ? j : bestj;
     }
+}
+
+// reduce_colors_inplace (s2tc_algorithm.cpp:363-414) for n = m = 16.  Between
+// two inputs the reference evaluates dist(c[lo], c[hi]) once and uses it both
+// ways; d(k, k) = 0.
+__device__ __forceinline__ void reduce16_rgb(const P* tp, Scratch16& sc, int& besti, int& bestj) {
+  const int t = threadIdx.x;
+  P pin[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    pin[i] = tp[in_slot(i)];
+    sc.pin[i][t] = pin[i];
+  }
+  int32_t S[120];
+#pragma unroll
+  for (int p = 0; p < 120; ++p) S[p] = 0;
+#pragma unroll 1
+  for (int k = 0; k < 16; ++k) {
+    const P pk = sc.pin[k][t];
+    int32_t col[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      col[i] = (kSymmetric || i < k) ? pdist<kMetric>(pin[i], pk) : pdist<kMetric>(pk, pin[i]);
+    int p = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+#pragma unroll
+      for (int j = i + 1; j < 16; ++j, ++p) S[p] = wadd(S[p], min(col[i], col[j]));
+  }
+  pick_pair(S, besti, bestj);
 }
 
 // reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) for n = m = 16
@@ -71,36 +102,30 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, int& besti, int& bestj
 // non-negative numbers is the square of their minimum, so the search runs on
 // absolute differences.  Its conditional write-back into c[0]/c[1] reads the
 // candidates before changing them, so the result is simply the winning pair.
-__device__ __forceinline__ void reduce16_alpha(const int* ain, int& besti, int& bestj) {
-  int A[16][16];
-  int F[16];
+__device__ __forceinline__ void reduce16_alpha(const int* ain, Scratch16& sc, int& besti, int& bestj) {
+  const int t = threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) F[k] = min(ain[k], 255 - ain[k]);
+  for (int i = 0; i < 16; ++i) sc.ain[i][t] = ain[i];
+  int32_t S[120];
 #pragma unroll
-  for (int i = 0; i < 16; ++i)
+  for (int p = 0; p < 120; ++p) S[p] = 0;
+#pragma unroll 1
+  for (int k = 0; k < 16; ++k) {
+    const int ak = sc.ain[k][t];
+    const int fk = min(ak, 255 - ak);
+    int col[16];
 #pragma unroll
-    for (int j = i + 1; j < 16; ++j) A[i][j] = abs(ain[i] - ain[j]);
-  int32_t bestsum = -1;
-  besti = 0;
-  bestj = 1;
+    for (int i = 0; i < 16; ++i) col[i] = min(abs(ain[i] - ak), fk);
+    int p = 0;
 #pragma unroll
-  for (int i = 0; i < 16; ++i)
+    for (int i = 0; i < 16; ++i)
 #pragma unroll
-    for (int j = i + 1; j < 16; ++j) {
-      int32_t sum = 0;
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        if (k == i || k == j) continue;
-        const int ai = k < i ? A[k][i] : A[i][k];
-        const int aj = k < j ? A[k][j] : A[j][k];
-        const int v = min(min(ai, aj), F[k]);
-        sum += v * v;
+      for (int j = i + 1; j < 16; ++j, ++p) {
+        const int v = min(col[i], col[j]);
+        S[p] += v * v;
       }
-      const bool take = bestsum < 0 || sum < bestsum;
-      bestsum = take ? sum : bestsum;
-      besti = take ? i : besti;
-      bestj = take ? j : bestj;
-    }
+  }
+  pick_pair(S, besti, bestj);
 }
 
 // ------------------------------------------------------------------------
@@ -213,13 +238,28 @@ struct EncodedBlock {
   uint64_t lo, hi;
 };
 
+// A block takes the full-block search when it has 16 inputs: all 16 texels
+// inside the image and, for DXT1, none of them transparent (the reference
+// leaves alpha-0 texels out of the candidate list, :947-949).
+template <int DXT>
+__device__ __forceinline__ bool is_full(const BlockTexels& bt) {
+  bool full = bt.w == 4 && bt.h == 4;
+  if (DXT == DXT1) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) full = full && (bt.px[i] >> 24) != 0;
+  }
+  return full;
+}
+
 // s2tc_encode_block<> (s2tc_algorithm.cpp:872-1108) for one block.
-// `prev_a1` is the second alpha endpoint left behind by the previous block of
-// the same image (used only by a single-texel DXT5 block without random
-// candidates); the return value is this block's leftover for the next one.
-template <int DXT, bool NORMAL, int REFINE>
+// FULL16 selects the register-resident search and requires a full block in
+// the all-texels mode without random candidates; otherwise the general search
+// runs.  `prev_a1` is the second alpha endpoint left behind by the previous
+// block of the same image (used only by a single-texel DXT5 block without
+// random candidates); the return value is this block's leftover for the next.
+template <int DXT, bool NORMAL, int REFINE, bool FULL16>
 __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* rnd, int prev_a1,
-                            EncodedBlock& out) {
+                            EncodedBlock& out, Scratch16& sc) {
   constexpr bool TRANS = DXT == DXT1;
   P tp[16];
 #pragma unroll
@@ -252,21 +292,16 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
         }
       }
   } else {
-    bool full = bt.w == 4 && bt.h == 4 && nrandom <= 0;
-    if (DXT == DXT1 && full) {
-#pragma unroll
-      for (int i = 0; i < 16; ++i) full = full && (bt.px[i] >> 24) != 0;
-    }
-    if (full) {
+    if constexpr (FULL16) {
       int bi, bj;
-      reduce16_rgb(tp, bi, bj);
+      reduce16_rgb(tp, sc, bi, bj);
       c0 = texel_c3(bt.px[(bi & 3) * 4 + (bi >> 2)]);
       c1 = texel_c3(bt.px[(bj & 3) * 4 + (bj >> 2)]);
       if (DXT == DXT5) {
         int ain[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) ain[k] = texel_a(bt.px[in_slot(k)]);
-        reduce16_alpha(ain, bi, bj);
+        reduce16_alpha(ain, sc, bi, bj);
         a0 = texel_a(bt.px[(bi & 3) * 4 + (bi >> 2)]);
         a1 = texel_a(bt.px[(bj & 3) * 4 + (bj >> 2)]);
       }
@@ -359,39 +394,10 @@ __device__ __forceinline__ void load_block(const uint32_t* __restrict__ t565, in
       bt.px[y * 4 + x] = (x < bt.w && y < bt.h) ? __ldg(p + size_t(y) * width + x) : 0u;
 }
 
-template <int DXT, bool NORMAL, int REFINE>
-__global__ void __launch_bounds__(128) k_encode(EncodeArgs a) {
-  const long long bl = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // block within this launch
-  if (bl >= (long long)a.bw * a.nby) return;
-  const long long b = (long long)a.by0 * a.bw + bl;                         // block within the image
-  const int by = int(b / a.bw), bx = int(b % a.bw);
-  BlockTexels bt;
-  load_block(a.t565, a.width, a.height, bx, by, bt);
-  const int per_block = a.nrandom > 0 ? a.nrandom * (DXT == DXT5 ? 4 : 3) : 0;
-  const uint32_t* rnd = a.rnd ? a.rnd + (size_t)bl * per_block : nullptr;
-  int prev_a1 = -1;
-  if (DXT == DXT5 && NORMAL && a.nrandom <= 0 && bt.w == 1 && bt.h == 1) {
-    // The reference encodes blocks in raster order into the same stack
-    // frame; a single-texel DXT5 block reads its second alpha candidate from
-    // a slot it never writes, i.e. the value the previous block left there
-    // (s2tc_algorithm.cpp:876, 996-1001).  That block is re-encoded here to
-    // recover it.
-    if (b > 0) {
-      const int pby = int((b - 1) / a.bw), pbx = int((b - 1) % a.bw);
-      BlockTexels pt;
-      load_block(a.t565, a.width, a.height, pbx, pby, pt);
-      EncodedBlock scratch;
-      prev_a1 = encode_block<DXT, NORMAL, REFINE>(pt, a.nrandom, nullptr, -1, scratch);
-    } else {
-      prev_a1 = a.prev_a1_first;
-    }
-  }
-  EncodedBlock eb;
-  const int leftover = encode_block<DXT, NORMAL, REFINE>(bt, a.nrandom, rnd, prev_a1, eb);
-  if (a.leftover_out && b == (long long)a.bw * a.bh - 1) *a.leftover_out = leftover;
-  uint8_t* o = a.dst + (size_t)by * a.pitch + (size_t)bx * (DXT == DXT1 ? 8 : 16);
+__device__ __forceinline__ void store_block(const EncodeArgs& a, int dxt, int bx, int by, const EncodedBlock& eb) {
+  uint8_t* o = a.dst + (size_t)by * a.pitch + (size_t)bx * (dxt == DXT1 ? 8 : 16);
   if (a.aligned) {
-    if (DXT == DXT1) {
+    if (dxt == DXT1) {
       *reinterpret_cast<uint64_t*>(o) = eb.lo;
     } else {
       *reinterpret_cast<ulonglong2*>(o) = make_ulonglong2(eb.lo, eb.hi);
@@ -399,19 +405,84 @@ __global__ void __launch_bounds__(128) k_encode(EncodeArgs a) {
   } else {
 #pragma unroll
     for (int i = 0; i < 8; ++i) o[i] = uint8_t(eb.lo >> (8 * i));
-    if (DXT != DXT1) {
+    if (dxt != DXT1) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) o[8 + i] = uint8_t(eb.hi >> (8 * i));
     }
   }
 }
 
+// Full blocks of the all-texels mode without random candidates.
+#ifndef S2TC_FULL16_MINBLOCKS
+#define S2TC_FULL16_MINBLOCKS 1
+#endif
+template <int DXT, int REFINE>
+__global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encode_full16(EncodeArgs a) {
+  __shared__ Scratch16 sc;
+  const long long bl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (bl >= (long long)a.bw * a.nby) return;
+  const long long b = (long long)a.by0 * a.bw + bl;
+  const int by = int(b / a.bw), bx = int(b % a.bw);
+  BlockTexels bt;
+  load_block(a.t565, a.width, a.height, bx, by, bt);
+  if (!is_full<DXT>(bt)) return;  // left to k_encode
+  EncodedBlock eb;
+  encode_block<DXT, true, REFINE, true>(bt, 0, nullptr, -1, eb, sc);
+  store_block(a, DXT, bx, by, eb);
+}
+
+// Every other block: the quick selection, random candidates, edge blocks and
+// DXT1 blocks with transparent texels.  In the all-texels mode without random
+// candidates the full blocks are skipped (k_encode_full16 encodes them).
+template <int DXT, bool NORMAL, int REFINE>
+__global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeArgs a) {
+  __shared__ Scratch16 sc;
+  const long long bl = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // block within this launch
+  if (bl >= (long long)a.bw * a.nby) return;
+  const long long b = (long long)a.by0 * a.bw + bl;                         // block within the image
+  const int by = int(b / a.bw), bx = int(b % a.bw);
+  BlockTexels bt;
+  load_block(a.t565, a.width, a.height, bx, by, bt);
+  if (NORMAL && a.nrandom <= 0 && is_full<DXT>(bt)) return;
+  const int per_block = a.nrandom > 0 ? a.nrandom * (DXT == DXT5 ? 4 : 3) : 0;
+  const uint32_t* rnd = a.rnd ? a.rnd + (size_t)bl * per_block : nullptr;
+  int prev_a1 = -1;
+  if (DXT == DXT5 && NORMAL && a.nrandom <= 0 && bt.w == 1 && bt.h == 1) {
+    // The reference encodes blocks in raster order into the same stack
+    // frame; a single-texel DXT5 block reads its second alpha candidate from
+    // a slot it never writes, i.e. the value the previous block left there
+    // (s2tc_algorithm.cpp:876, 996-1001).  That block is re-encoded here (the
+    // general search gives the same bytes as the full-block one) to recover it.
+    if (b > 0) {
+      const int pby = int((b - 1) / a.bw), pbx = int((b - 1) % a.bw);
+      BlockTexels pt;
+      load_block(a.t565, a.width, a.height, pbx, pby, pt);
+      EncodedBlock scratch;
+      prev_a1 = encode_block<DXT, NORMAL, REFINE, false>(pt, a.nrandom, nullptr, -1, scratch, sc);
+    } else {
+      prev_a1 = a.prev_a1_first;
+    }
+  }
+  EncodedBlock eb;
+  const int leftover = encode_block<DXT, NORMAL, REFINE, false>(bt, a.nrandom, rnd, prev_a1, eb, sc);
+  if (a.leftover_out && b == (long long)a.bw * a.bh - 1) *a.leftover_out = leftover;
+  store_block(a, DXT, bx, by, eb);
+}
+
 template <int DXT, bool NORMAL>
 cudaError_t launch_r(const EncodeArgs& a, int refine, cudaStream_t s) {
   const long long nb = (long long)a.bw * a.nby;
   if (nb == 0) return cudaSuccess;
-  const int threads = 128;
+  const int threads = kThreadsPerCta;
   const unsigned grid = unsigned((nb + threads - 1) / threads);
+  if (NORMAL && a.nrandom <= 0) {
+    count_launches(1);
+    switch (refine) {
+      case RF_NEVER: k_encode_full16<DXT, RF_NEVER><<<grid, threads, 0, s>>>(a); break;
+      case RF_LOOP: k_encode_full16<DXT, RF_LOOP><<<grid, threads, 0, s>>>(a); break;
+      default: k_encode_full16<DXT, RF_ALWAYS><<<grid, threads, 0, s>>>(a); break;
+    }
+  }
   count_launches(1);
   switch (refine) {
     case RF_NEVER: k_encode<DXT, NORMAL, RF_NEVER><<<grid, threads, 0, s>>>(a); break;
