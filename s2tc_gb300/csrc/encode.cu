@@ -10,6 +10,8 @@
 // DXT1/DXT3/DXT5 blocks, block rows `pitch` bytes apart.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "dither.h"
 #include "encode.h"
 #include "s2tc_device.cuh"
@@ -469,12 +471,445 @@ __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeArgs a) {
   store_block(a, DXT, bx, by, eb);
 }
 
+// ------------------------------------------------------------------------
+// Random candidates: one warp per block.
+//
+// The candidate list (the block's inputs, then nrandom random colours) and
+// each candidate's distance row against the inputs live in shared memory.
+// Lane l owns the rows i = l, l + 32, ...; all lanes walk j together, so the
+// row-j loads are broadcasts.  Without negative sums (they need the SRGB
+// metrics' int32 wrap-around) the reference's `bestsum < 0 || sum < bestsum`
+// rule picks the first pair with the smallest sum, i.e. the smallest
+// (sum, i, j); a block that sees a negative sum is replayed by one lane in
+// exact sequential order.  Refinement runs with one lane per texel and warp
+// reductions.
+
+constexpr int kRandWarps = 4;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+struct RandLayout {
+  size_t p, c, a, d, e, bytes;  // section offsets and bytes per warp
+};
+
+__host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+__host__ __device__ __forceinline__ RandLayout rand_layout(int m) {
+  RandLayout L;
+  L.p = 0;
+  L.c = align16(L.p + size_t(m) * sizeof(P));          // prepared candidates
+  L.a = align16(L.c + size_t(m) * sizeof(uint16_t));   // candidate colours, 5:6:5
+  L.d = align16(L.a + size_t(m));                       // candidate alphas
+  L.e = align16(L.d + size_t(m) * 16 * sizeof(int32_t));  // colour distance rows
+  L.bytes = align16(L.e + size_t(m) * 16);              // alpha rows (bytes)
+  return L;
+}
+
+__device__ __forceinline__ C3 unpack565(uint32_t v) { return C3{int(v >> 11) & 31, int(v >> 5) & 63, int(v) & 31}; }
+
+// One colour index pass over the block, lane s (< 16) holding slot s.
+struct WarpColourPass {
+  uint32_t bits, score;
+  int n0, n1, s0r, s0g, s0b, s1r, s1g, s1b;
+};
+
+template <bool TRANS, bool ACC>
+__device__ __forceinline__ WarpColourPass colour_pass_warp(bool inb, uint32_t px, const P& tp, C3 r0, C3 r1,
+                                                          int lane) {
+  WarpColourPass o;
+  const P p0 = prep<kMetric>(r0), p1 = prep<kMetric>(r1);
+  const bool trans = TRANS && inb && (px >> 24) == 0;
+  const bool active = inb && !trans;
+  int32_t d0 = 0, d1 = 0;
+  if (active) {
+    d0 = pdist<kMetric>(tp, p0);
+    d1 = pdist<kMetric>(tp, p1);
+  }
+  const bool one = active && d1 < d0;
+  const uint32_t idx = trans ? 3u : (one ? 1u : 0u);
+  o.bits = __reduce_or_sync(kFull, lane < 16 ? idx << (2 * lane) : 0u);
+  o.score = __reduce_add_sync(kFull, active ? uint32_t(one ? d1 : d0) : 0u);
+  if (ACC) {
+    const C3 c = texel_c3(px);
+    o.n1 = __popc(__ballot_sync(kFull, one));
+    o.n0 = __popc(__ballot_sync(kFull, active && !one));
+    o.s1r = int(__reduce_add_sync(kFull, one ? uint32_t(c.r) : 0u));
+    o.s1g = int(__reduce_add_sync(kFull, one ? uint32_t(c.g) : 0u));
+    o.s1b = int(__reduce_add_sync(kFull, one ? uint32_t(c.b) : 0u));
+    o.s0r = int(__reduce_add_sync(kFull, active && !one ? uint32_t(c.r) : 0u));
+    o.s0g = int(__reduce_add_sync(kFull, active && !one ? uint32_t(c.g) : 0u));
+    o.s0b = int(__reduce_add_sync(kFull, active && !one ? uint32_t(c.b) : 0u));
+  }
+  return o;
+}
+
+__device__ __forceinline__ bool warp_means(const WarpColourPass& a, C3& c0, C3& c1) {
+  if (!a.n0 && !a.n1) return false;
+  if (a.n0) c0 = C3{rmean(a.s0r, a.n0) & 31, rmean(a.s0g, a.n0) & 63, rmean(a.s0b, a.n0) & 31};
+  if (a.n1) c1 = C3{rmean(a.s1r, a.n1) & 31, rmean(a.s1g, a.n1) & 63, rmean(a.s1b, a.n1) & 31};
+  return true;
+}
+
+// colour_refine (s2tc_algorithm.cpp:767-860), warp-parallel; results uniform.
+template <bool TRANS, int REFINE>
+__device__ __forceinline__ uint32_t colour_refine_warp(bool inb, uint32_t px, const P& tp, C3& c0, C3& c1,
+                                                       int lane) {
+  uint32_t bits = 0;
+  if (REFINE == RF_NEVER) {
+    if (TRANS ? c3_lt(c1, c0) : c3_lt(c0, c1)) {
+      C3 t = c0; c0 = c1; c1 = t;
+    }
+    return colour_pass_warp<TRANS, false>(inb, px, tp, c0, c1, lane).bits;
+  } else if (REFINE == RF_LOOP) {
+    C3 n0 = c0, n1 = c1;
+    uint32_t best = 0x7FFFFFFFu;
+    for (;;) {
+      const WarpColourPass r = colour_pass_warp<TRANS, true>(inb, px, tp, n0, n1, lane);
+      if (!(r.score < best)) break;
+      bits = r.bits;
+      best = r.score;
+      c0 = n0;
+      c1 = n1;
+      if (!warp_means(r, n0, n1)) break;
+    }
+  } else {
+    const WarpColourPass r = colour_pass_warp<TRANS, true>(inb, px, tp, c0, c1, lane);
+    bits = r.bits;
+    warp_means(r, c0, c1);
+  }
+  colour_finish<TRANS>(bits, c0, c1);
+  return bits;
+}
+
+struct WarpAlphaPass {
+  uint64_t bits;
+  uint32_t score;
+  int n0, n1, s0, s1;
+};
+
+// alpha index pass with the 0/255 fixed points (s2tc_algorithm.cpp:582-643)
+template <bool ACC>
+__device__ __forceinline__ WarpAlphaPass alpha_pass_warp(bool inb, uint32_t px, int r0, int r1, int lane) {
+  WarpAlphaPass o;
+  const int a = int(px >> 24);
+  uint32_t idx = 0, d = 0;
+  bool e0 = false, e1 = false;
+  if (inb) {
+    int32_t bd = adist(a, r0), d1 = adist(a, r1);
+    int best = 0;
+    if (d1 < bd) { bd = d1; best = 1; }
+    const int32_t dz = a * a, df = (255 - a) * (255 - a);
+    if (dz <= bd) { idx = 6; d = uint32_t(dz); }
+    else if (df <= bd) { idx = 7; d = uint32_t(df); }
+    else { idx = uint32_t(best); d = uint32_t(bd); e0 = best == 0; e1 = best == 1; }
+  }
+  const uint32_t lo = __reduce_or_sync(kFull, lane < 10 ? idx << (3 * lane) : 0u);
+  const uint32_t hi = __reduce_or_sync(kFull, (lane >= 10 && lane < 16) ? idx << (3 * (lane - 10)) : 0u);
+  o.bits = uint64_t(lo) | (uint64_t(hi) << 30);
+  o.score = __reduce_add_sync(kFull, d);
+  if (ACC) {
+    o.n0 = __popc(__ballot_sync(kFull, e0));
+    o.n1 = __popc(__ballot_sync(kFull, e1));
+    o.s0 = int(__reduce_add_sync(kFull, e0 ? uint32_t(a) : 0u));
+    o.s1 = int(__reduce_add_sync(kFull, e1 ? uint32_t(a) : 0u));
+  }
+  return o;
+}
+
+// alpha_refine (s2tc_algorithm.cpp:645-765), warp-parallel; results uniform.
+template <int REFINE>
+__device__ __forceinline__ uint64_t alpha_refine_warp(bool inb, uint32_t px, int& a0, int& a1, int lane) {
+  uint64_t bits = 0;
+  if (REFINE == RF_NEVER) {
+    if (a1 < a0) { int t = a0; a0 = a1; a1 = t; }
+    return alpha_pass_warp<false>(inb, px, a0, a1, lane).bits;
+  } else if (REFINE == RF_LOOP) {
+    int x0 = a0, x1 = a1;
+    uint32_t best = 0x7FFFFFFFu;
+    for (;;) {
+      const WarpAlphaPass r = alpha_pass_warp<true>(inb, px, x0, x1, lane);
+      if (!(r.score < best)) break;
+      bits = r.bits;
+      best = r.score;
+      a0 = x0;
+      a1 = x1;
+      if (!r.n0 && !r.n1) break;
+      if (r.n0) x0 = rmean(r.s0, r.n0) & 255;
+      if (r.n1) x1 = rmean(r.s1, r.n1) & 255;
+    }
+  } else {
+    const WarpAlphaPass r = alpha_pass_warp<true>(inb, px, a0, a1, lane);
+    bits = r.bits;
+    if (r.n0) a0 = rmean(r.s0, r.n0) & 255;
+    if (r.n1) a1 = rmean(r.s1, r.n1) & 255;
+  }
+  alpha_finish(bits, a0, a1);
+  return bits;
+}
+
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t w = __shfl_xor_sync(kFull, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+
+template <int DXT, int REFINE>
+__global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeArgs a, int m) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const RandLayout L = rand_layout(m);
+  unsigned char* base = smem + size_t(warp) * L.bytes;
+  P* sP = reinterpret_cast<P*>(base + L.p);
+  uint16_t* sC = reinterpret_cast<uint16_t*>(base + L.c);
+  uint8_t* sA = base + L.a;
+  int32_t* sD = reinterpret_cast<int32_t*>(base + L.d);
+  uint8_t* sE = base + L.e;
+  const int nrandom = a.nrandom;
+  const int stride = DXT == DXT5 ? 4 : 3;
+  const long long nb = (long long)a.bw * a.nby;
+
+  for (long long bl = (long long)blockIdx.x * kRandWarps + warp; bl < nb; bl += (long long)gridDim.x * kRandWarps) {
+    const long long b = (long long)a.by0 * a.bw + bl;
+    const int by = int(b / a.bw), bx = int(b % a.bw);
+    const int bw_ = min(4, a.width - bx * 4), bh_ = min(4, a.height - by * 4);
+    // lanes 0..15 hold the block's slots (y*4 + x)
+    const int sx = lane & 3, sy = (lane >> 2) & 3;
+    const bool inb = lane < 16 && sx < bw_ && sy < bh_;
+    uint32_t px = 0;
+    if (inb) px = __ldg(a.t565 + (size_t(by) * 4 + sy) * a.width + size_t(bx) * 4 + sx);
+    const bool valid = inb && !(DXT == DXT1 && (px >> 24) == 0);
+    const int pos = sx * 4 + sy;  // x-outer, y-inner input order (:940-951)
+    const unsigned mask = __reduce_or_sync(kFull, valid ? 1u << pos : 0u);
+    int n = __popc(mask);
+    const C3 c = texel_c3(px);
+    const P tp = prep<kMetric>(c);
+    if (valid) {
+      const int rank = __popc(mask & ((1u << pos) - 1u));
+      sP[rank] = tp;
+      sC[rank] = uint16_t(pack565(c));
+      sA[rank] = uint8_t(px >> 24);
+    }
+    // bounding box of the inputs (:962-983); an empty block has one black input
+    C3 lo, hi;
+    lo.r = int(__reduce_min_sync(kFull, valid ? unsigned(c.r) : 255u));
+    lo.g = int(__reduce_min_sync(kFull, valid ? unsigned(c.g) : 255u));
+    lo.b = int(__reduce_min_sync(kFull, valid ? unsigned(c.b) : 255u));
+    hi.r = int(__reduce_max_sync(kFull, valid ? unsigned(c.r) : 0u));
+    hi.g = int(__reduce_max_sync(kFull, valid ? unsigned(c.g) : 0u));
+    hi.b = int(__reduce_max_sync(kFull, valid ? unsigned(c.b) : 0u));
+    int alo = 0, ahi = 0;
+    if (DXT == DXT5) {
+      alo = int(__reduce_min_sync(kFull, valid ? (px >> 24) : 255u));
+      ahi = int(__reduce_max_sync(kFull, valid ? (px >> 24) : 0u));
+    }
+    if (n == 0) {
+      n = 1;
+      lo = hi = C3{0, 0, 0};
+      alo = ahi = 0;
+      if (lane == 0) {
+        sP[0] = prep<kMetric>(C3{0, 0, 0});
+        sC[0] = 0;
+        sA[0] = 0;
+      }
+    }
+    const int mm = n + nrandom;
+    const int lr = hi.r - lo.r + 1, lg = hi.g - lo.g + 1, lb = hi.b - lo.b + 1, la = ahi - alo + 1;
+    // random candidates (:984-992), rand() words in the reference's call order
+    const uint32_t* rnd = a.rnd + size_t(bl) * size_t(nrandom) * stride;
+    for (int j = n + lane; j < mm; j += 32) {
+      const uint32_t* r = rnd + size_t(j - n) * stride;
+      const C3 cj{lo.r + int(__ldg(r) % uint32_t(lr)), lo.g + int(__ldg(r + 1) % uint32_t(lg)),
+                  lo.b + int(__ldg(r + 2) % uint32_t(lb))};
+      sP[j] = prep<kMetric>(cj);
+      sC[j] = uint16_t(pack565(cj));
+      if (DXT == DXT5) sA[j] = uint8_t(alo + int(__ldg(r + 3) % uint32_t(la)));
+    }
+    __syncwarp();
+    // distance rows against the inputs (:375-392); entries k >= n are 0
+    for (int i = lane; i < mm; i += 32) {
+      const P pi = sP[i];
+      int32_t row[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        int32_t d = 0;
+        if (k < n && k != i) {
+          const P pk = sP[k];
+          d = (kSymmetric || i >= n || i < k) ? pdist<kMetric>(pi, pk) : pdist<kMetric>(pk, pi);
+        }
+        row[k] = d;
+      }
+      int4* dr = reinterpret_cast<int4*>(sD + size_t(i) * 16);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dr[q] = make_int4(row[4 * q], row[4 * q + 1], row[4 * q + 2], row[4 * q + 3]);
+      if (DXT == DXT5) {
+        const int ai = sA[i];
+        uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          if (k < n) {
+            const int ak = sA[k];
+            const uint32_t v = uint32_t(min(abs(ai - ak), min(ak, 255 - ak)));
+            w[k >> 2] |= v << (8 * (k & 3));
+          }
+        }
+        *reinterpret_cast<uint4*>(sE + size_t(i) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    }
+    __syncwarp();
+
+    // colour pair search
+    int ci, cj;
+    {
+      uint64_t best = ~0ull;
+      bool neg = false;
+      for (int r0 = 0; r0 < mm; r0 += 32) {
+        const int i = r0 + lane;
+        int32_t ri[16];
+        if (i < mm) {
+          const int4* q = reinterpret_cast<const int4*>(sD + size_t(i) * 16);
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int4 v = q[t];
+            ri[4 * t] = v.x; ri[4 * t + 1] = v.y; ri[4 * t + 2] = v.z; ri[4 * t + 3] = v.w;
+          }
+        }
+        for (int j = r0 + 1; j < mm; ++j) {
+          const int4* q = reinterpret_cast<const int4*>(sD + size_t(j) * 16);
+          int32_t sum = 0;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int4 v = q[t];
+            sum = wadd(sum, min(ri[4 * t], v.x));
+            sum = wadd(sum, min(ri[4 * t + 1], v.y));
+            sum = wadd(sum, min(ri[4 * t + 2], v.z));
+            sum = wadd(sum, min(ri[4 * t + 3], v.w));
+          }
+          if (i < mm && j > i) {
+            neg |= sum < 0;
+            const uint64_t key = (uint64_t(uint32_t(sum)) << 32) | (uint32_t(i) << 16) | uint32_t(j);
+            if (sum >= 0 && key < best) best = key;
+          }
+        }
+      }
+      if (__any_sync(kFull, neg)) {
+        // negative sums: replay the reference's rule in pair order on one lane
+        int bi = 0, bj = 1;
+        if (lane == 0) {
+          int32_t bestsum = -1;
+          for (int i = 0; i < mm; ++i)
+            for (int j = i + 1; j < mm; ++j) {
+              int32_t sum = 0;
+              for (int k = 0; k < 16; ++k) sum = wadd(sum, min(sD[i * 16 + k], sD[j * 16 + k]));
+              if (bestsum < 0 || sum < bestsum) {
+                bestsum = sum;
+                bi = i;
+                bj = j;
+              }
+            }
+        }
+        ci = __shfl_sync(kFull, bi, 0);
+        cj = __shfl_sync(kFull, bj, 0);
+      } else {
+        best = warp_min_u64(best);
+        ci = int((best >> 16) & 0xFFFF);
+        cj = int(best & 0xFFFF);
+      }
+    }
+    C3 c0 = unpack565(sC[ci]), c1 = unpack565(sC[cj]);
+    int a0 = 0, a1 = 0;
+    if (DXT == DXT5) {
+      // alpha pair search (:415-478); sums of squares of bytes never overflow
+      uint64_t best = ~0ull;
+      for (int r0 = 0; r0 < mm; r0 += 32) {
+        const int i = r0 + lane;
+        uint4 ri = make_uint4(0, 0, 0, 0);
+        if (i < mm) ri = *reinterpret_cast<const uint4*>(sE + size_t(i) * 16);
+        for (int j = r0 + 1; j < mm; ++j) {
+          const uint4 rj = *reinterpret_cast<const uint4*>(sE + size_t(j) * 16);
+          uint32_t v, sum = 0;
+          v = __vminu4(ri.x, rj.x); sum = __dp4a(v, v, sum);
+          v = __vminu4(ri.y, rj.y); sum = __dp4a(v, v, sum);
+          v = __vminu4(ri.z, rj.z); sum = __dp4a(v, v, sum);
+          v = __vminu4(ri.w, rj.w); sum = __dp4a(v, v, sum);
+          if (i < mm && j > i) {
+            const uint64_t key = (uint64_t(sum) << 32) | (uint32_t(i) << 16) | uint32_t(j);
+            if (key < best) best = key;
+          }
+        }
+      }
+      best = warp_min_u64(best);
+      a0 = sA[(best >> 16) & 0xFFFF];
+      a1 = sA[best & 0xFFFF];
+    }
+    __syncwarp();  // the next block overwrites the candidate lists
+
+    // equal endpoints are bumped apart (:1009-1027)
+    if (c3_eq(c0, c1)) c1 = (c0.r == 31 && c0.g == 63 && c0.b == 31) ? c3_prev(c1) : c3_next(c1);
+    if (DXT == DXT5 && a0 == a1) {
+      if (a0 == 255) --a1; else ++a1;
+    }
+    const uint32_t cbits = colour_refine_warp<DXT == DXT1, REFINE>(inb, px, tp, c0, c1, lane);
+    EncodedBlock eb;
+    const uint64_t colour = uint64_t(pack565(c0)) | (uint64_t(pack565(c1)) << 16) | (uint64_t(cbits) << 32);
+    if (DXT == DXT1) {
+      eb.lo = colour;
+      eb.hi = 0;
+    } else if (DXT == DXT3) {
+      const uint32_t nib = inb ? ((px >> 24) & 15) : 0u;
+      const uint32_t lo32 = __reduce_or_sync(kFull, lane < 8 ? nib << (4 * lane) : 0u);
+      const uint32_t hi32 = __reduce_or_sync(kFull, (lane >= 8 && lane < 16) ? nib << (4 * (lane - 8)) : 0u);
+      eb.lo = uint64_t(lo32) | (uint64_t(hi32) << 32);
+      eb.hi = colour;
+    } else {
+      const uint64_t abits = alpha_refine_warp<REFINE>(inb, px, a0, a1, lane);
+      eb.lo = uint64_t(a0) | (uint64_t(a1) << 8) | (abits << 16);
+      eb.hi = colour;
+    }
+    if (lane == 0) store_block(a, DXT, bx, by, eb);
+  }
+}
+
+// Shared memory the warp kernel needs for `m` candidates, or 0 when it does
+// not fit (the thread-per-block kernel then handles the launch).
+size_t rand_smem_bytes(int m) {
+  const size_t bytes = rand_layout(m).bytes * kRandWarps;
+  return bytes <= 200 * 1024 ? bytes : 0;
+}
+
 template <int DXT, bool NORMAL>
 cudaError_t launch_r(const EncodeArgs& a, int refine, cudaStream_t s) {
   const long long nb = (long long)a.bw * a.nby;
   if (nb == 0) return cudaSuccess;
   const int threads = kThreadsPerCta;
   const unsigned grid = unsigned((nb + threads - 1) / threads);
+  if (NORMAL && a.nrandom > 0) {
+    const int m = 16 + a.nrandom;
+    const size_t smem = rand_smem_bytes(m);
+    if (smem > 0) {
+      count_launches(1);
+      const unsigned rgrid = unsigned(std::min<long long>((nb + kRandWarps - 1) / kRandWarps, 152ll * 64));
+      cudaError_t e = cudaSuccess;
+      switch (refine) {
+        case RF_NEVER:
+          e = cudaFuncSetAttribute(k_encode_rand<DXT, RF_NEVER>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+          if (e == cudaSuccess) k_encode_rand<DXT, RF_NEVER><<<rgrid, 32 * kRandWarps, smem, s>>>(a, m);
+          break;
+        case RF_LOOP:
+          e = cudaFuncSetAttribute(k_encode_rand<DXT, RF_LOOP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+          if (e == cudaSuccess) k_encode_rand<DXT, RF_LOOP><<<rgrid, 32 * kRandWarps, smem, s>>>(a, m);
+          break;
+        default:
+          e = cudaFuncSetAttribute(k_encode_rand<DXT, RF_ALWAYS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(smem));
+          if (e == cudaSuccess) k_encode_rand<DXT, RF_ALWAYS><<<rgrid, 32 * kRandWarps, smem, s>>>(a, m);
+          break;
+      }
+      if (e != cudaSuccess) return e;
+      return cudaGetLastError();
+    }
+  }
   if (NORMAL && a.nrandom <= 0) {
     count_launches(1);
     switch (refine) {

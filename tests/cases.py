@@ -7,10 +7,23 @@ FORMATS = (0x83F0, 0x83F1, 0x83F2, 0x83F3)
 NRANDOM = (-1, 0, 1, 2, 7, 16)
 
 
+# 8-bit colours whose 5:6:5 truncations are magenta-like and green-like
+# extremes; the SRGB metric's int32 arithmetic wraps between such colours and
+# gives negative distances (e.g. (31,0,31) vs (5,60,3)).
+SRGB_WRAP_COLOURS = np.array([[248, 0, 248], [40, 240, 24], [248, 44, 248], [8, 244, 8], [16, 240, 0],
+                              [248, 76, 248], [0, 252, 0], [248, 16, 240]], np.uint8)
+
+
 def image(rng: np.random.Generator, w: int, h: int, sc: int, kind: int | None = None) -> np.ndarray:
     """Small test image with one of several value distributions (uniform,
-    extremes, coarse levels, flat, alpha-heavy)."""
-    kind = int(rng.integers(0, 5)) if kind is None else kind
+    extremes, coarse levels, flat, alpha-heavy, SRGB wrap-around colours)."""
+    kind = int(rng.integers(0, 6)) if kind is None else kind
+    if kind == 5:
+        img = np.empty((w * h, sc), np.uint8)
+        img[:, :3] = SRGB_WRAP_COLOURS[rng.integers(0, len(SRGB_WRAP_COLOURS), w * h)]
+        if sc == 4:
+            img[:, 3] = rng.choice(np.array([255, 255, 0, 128], np.uint8), w * h)
+        return img.reshape(-1)
     n = w * h * sc
     if kind == 0:
         return rng.integers(0, 256, n, dtype=np.uint8)

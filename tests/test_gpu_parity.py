@@ -42,6 +42,38 @@ def test_random_sweep(lib, oracle):
         assert np.array_equal(a, b), (w, h, sc, hex(fmt), dither, metric, nr, refine)
 
 
+def test_srgb_wraparound(lib, oracle):
+    """SRGB distances that wrap negative: the full-block kernel, the warp
+    kernel's sequential fallback and the thread kernel all keep the
+    reference's `bestsum < 0` rule."""
+    rng = np.random.default_rng(23)
+    for it in range(200):
+        w, h = int(rng.integers(1, 24)), int(rng.integers(1, 24))
+        fmt = int(rng.choice(cases.FORMATS))
+        nr = int(rng.choice([-1, 0, 3, 40]))
+        metric = int(rng.choice([2, 2, 3]))
+        refine = int(rng.integers(0, 3))
+        img = cases.image(rng, w, h, 4, 5)
+        a = gpu_compress(4, w, h, img, fmt, 0, metric, nr, refine, it + 1)
+        b = oracle.compress(4, w, h, img, fmt, 0, metric, nr, refine, seed=it + 1)
+        assert np.array_equal(a, b), (w, h, hex(fmt), metric, nr, refine)
+
+
+@pytest.mark.parametrize("nr", [64, 300, 700])
+def test_many_random_candidates(lib, oracle, nr):
+    """Random-candidate counts served by the warp kernel (shared-memory
+    candidate lists) and, past its shared-memory limit, by the thread kernel."""
+    rng = np.random.default_rng(nr)
+    for fmt in (0x83F1, 0x83F2, 0x83F3):
+        for metric in (5, 3, 7, 2):
+            w, h = int(rng.integers(5, 20)), int(rng.integers(5, 20))
+            img = cases.image(rng, w, h, 4)
+            refine = int(rng.integers(0, 3))
+            a = gpu_compress(4, w, h, img, fmt, 1, metric, nr, refine, 7)
+            b = oracle.compress(4, w, h, img, fmt, 1, metric, nr, refine, seed=7)
+            assert np.array_equal(a, b), (hex(fmt), metric, refine)
+
+
 @pytest.mark.parametrize("fmt", cases.FORMATS)
 def test_every_small_size(lib, oracle, fmt):
     rng = np.random.default_rng(fmt + 1)

@@ -91,6 +91,22 @@ def test_corner_leftover_rule(oracle, reference):
         assert np.array_equal(a, b), (w, h, metric, refine, nr)
 
 
+def test_srgb_wraparound(oracle, reference):
+    """Images of colours whose SRGB distances wrap negative: exercises the
+    reference's `bestsum < 0` rule and its wrap-around arithmetic."""
+    rng = np.random.default_rng(17)
+    for it in range(300):
+        w, h = int(rng.integers(1, 13)), int(rng.integers(1, 13))
+        fmt = int(rng.choice(cases.FORMATS))
+        nr = int(rng.choice([-1, 0, 3, 40]))
+        metric = int(rng.choice([2, 2, 3]))
+        if cases.is_unpinned_corner(w, h, fmt, metric, nr):
+            continue
+        img = cases.image(rng, w, h, 4, 5)
+        a, b = _both(oracle, reference, w, h, 4, fmt, 0, metric, nr, int(rng.integers(0, 3)), img, it + 1)
+        assert np.array_equal(a, b), (w, h, hex(fmt), metric, nr)
+
+
 def test_wrapv_twin_agrees(reference):
     """The reference built with -fwrapv gives the same bytes, so gcc does not
     exploit the SRGB metric's signed overflow: the encoder's arithmetic is
