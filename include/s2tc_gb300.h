@@ -105,6 +105,36 @@ void s2tc_options_from_env(s2tc_options *opt);
 int s2tc_gpu_compress(int srccomps, int width, int height, const void *d_src, unsigned int destformat, void *d_dst,
 		      long long dst_pitch, const s2tc_options *opt, const unsigned int *d_rand, void *stream);
 
+/* ---- batches: many images (textures, mip levels) of uneven sizes ---- */
+
+/* One image of a batch: device pointers, as for s2tc_gpu_compress.  `rand`
+ * optionally gives the image's replayed rand() words (nrandom*(3|4) per block
+ * in raster order); when NULL and the knobs select random candidates, each run
+ * draws them from libc rand() on the host, in image order, as one
+ * tx_compress_dxtn call per image would. */
+typedef struct s2tc_image {
+	const void *src;
+	int width, height, srccomps;
+	unsigned int format;
+	void *dst;
+	long long dst_pitch;
+	const unsigned int *rand;
+} s2tc_image;
+
+typedef struct s2tc_batch s2tc_batch;
+
+/* Plan a batch: allocates the device scratch and tables for all images and
+ * captures the whole launch sequence (the dither of every image, then one
+ * encoder launch per block format) in a CUDA graph.  The images' pointers and
+ * sizes are fixed for the plan; their contents may change between runs. */
+int s2tc_batch_create(s2tc_batch **out, const s2tc_image *items, int count, const s2tc_options *opt);
+/* Replay the plan on `stream` (NULL: the library's stream); asynchronous.
+ * Runs of one plan are serialised. */
+int s2tc_batch_run(s2tc_batch *batch, void *stream);
+/* Number of kernels one run launches. */
+int s2tc_batch_kernels(const s2tc_batch *batch);
+void s2tc_batch_destroy(s2tc_batch *batch);
+
 /* Wait for `stream` (NULL: the library's stream) and report whether any
  * kernel since the last check gave up a bounded wait (S2TC_ERR_TIMEOUT). */
 int s2tc_gpu_synchronize(void *stream);

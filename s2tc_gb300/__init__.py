@@ -45,6 +45,13 @@ class S2tcError(RuntimeError):
     pass
 
 
+class Image(ctypes.Structure):
+    """``s2tc_image``: one image of a batch (device pointers)."""
+    _fields_ = [("src", ctypes.c_void_p), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("srccomps", ctypes.c_int), ("format", ctypes.c_uint), ("dst", ctypes.c_void_p),
+                ("dst_pitch", ctypes.c_longlong), ("rand", ctypes.c_void_p)]
+
+
 class Options(ctypes.Structure):
     """``s2tc_options``: the S2TC_* knobs as a struct."""
     _fields_ = [("dither", ctypes.c_int), ("metric", ctypes.c_int),
@@ -107,6 +114,15 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_gpu_stage_ms.restype = c_int
     lib.s2tc_gpu_kernel_launches.argtypes = []
     lib.s2tc_gpu_kernel_launches.restype = c_ll
+    lib.s2tc_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Image), c_int,
+                                      ctypes.POINTER(Options)]
+    lib.s2tc_batch_create.restype = c_int
+    lib.s2tc_batch_run.argtypes = [vp, vp]
+    lib.s2tc_batch_run.restype = c_int
+    lib.s2tc_batch_kernels.argtypes = [vp]
+    lib.s2tc_batch_kernels.restype = c_int
+    lib.s2tc_batch_destroy.argtypes = [vp]
+    lib.s2tc_batch_destroy.restype = None
     lib.s2tc_last_error.argtypes = []
     lib.s2tc_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -120,7 +136,8 @@ EXPORTED_SYMBOLS = (
     "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5", "rgb565_image",
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
     "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
-    "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc",
+    "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run",
+    "s2tc_batch_kernels", "s2tc_batch_destroy",
     "s2tc_last_error",
 )
 
@@ -267,6 +284,56 @@ def gpu_compress_noalloc(srccomps: int, width: int, height: int, d_src, destform
     rnd_p = None if d_rand is None else (d_rand if isinstance(d_rand, int) else _ptr(d_rand))
     return int(load().s2tc_gpu_compress_noalloc(srccomps, width, height, src_p, destformat, dst_p, dst_pitch,
                                                 ctypes.byref(opt), rnd_p, stream))
+
+
+class Batch:
+    """A planned batch (``s2tc_batch_create``): images of uneven sizes and
+    mixed formats encoded by one CUDA-graph launch per ``run``.
+
+    ``images`` is a list of dicts with keys src, width, height, srccomps,
+    format, dst and optionally dst_pitch and rand (device tensors or raw
+    pointers)."""
+
+    def __init__(self, images, opt: Options):
+        arr = (Image * max(1, len(images)))()
+        self._keep = []
+        for i, im in enumerate(images):
+            w, h, fmt = int(im["width"]), int(im["height"]), int(im["format"])
+            pitch = im.get("dst_pitch") or ((w + 3) // 4) * block_bytes(fmt)
+            rnd = im.get("rand")
+            arr[i] = Image(_addr(im["src"]), w, h, int(im["srccomps"]), fmt, _addr(im["dst"]), int(pitch),
+                           None if rnd is None else _addr(rnd))
+            self._keep.append(im)
+        self._opt = opt
+        h = ctypes.c_void_p()
+        st = load().s2tc_batch_create(ctypes.byref(h), arr, len(images), ctypes.byref(opt))
+        if st != S2TC_OK:
+            raise S2tcError(f"s2tc_batch_create failed ({st}): {last_error()}")
+        self.handle = h
+
+    @property
+    def kernels(self) -> int:
+        return int(load().s2tc_batch_kernels(self.handle))
+
+    def run(self, stream: int | None = None) -> None:
+        st = load().s2tc_batch_run(self.handle, stream)
+        if st != S2TC_OK:
+            raise S2tcError(f"s2tc_batch_run failed ({st}): {last_error()}")
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            load().s2tc_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _addr(x) -> int:
+    return x if isinstance(x, int) else _ptr(x)
 
 
 def gpu_synchronize(stream: int | None = None) -> None:

@@ -310,6 +310,219 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
   cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
 
+
+// ------------------------------------------------------------------ batches
+
+// A planned batch: device tables, scratch and a CUDA graph of the whole
+// launch sequence (dither for every image, then the encoder kernels of each
+// format), replayed by s2tc_batch_run.
+struct Batch {
+  std::vector<s2tc_image> items;  // images with at least one texel
+  s2tc_options opt;
+  bool normal = false;
+  DevBuf t565, scratch, tables, rnd;
+  PinnedBuf host_rnd;
+  long long host_rand_words = 0;        // rand words replayed per run (host path)
+  std::vector<long long> rand_words;    // per image
+  cudaStream_t capture = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;
+  int kernels = 0;                      // kernels per run
+  // prepared launch descriptors (device tables already uploaded)
+  DitherWork dwork{};
+  std::vector<DitherArgs> fs_items;     // Floyd-Steinberg: one launch per image
+  std::vector<size_t> fs_off;
+  EncodeWork ework[3]{};
+  bool has_fmt[3] = {false, false, false};
+
+  ~Batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (done) cudaEventDestroy(done);
+    if (capture) cudaStreamDestroy(capture);
+    for (DevBuf* b : {&t565, &scratch, &tables, &rnd})
+      if (b->p) cudaFree(b->p);
+    if (host_rnd.p) cudaFreeHost(host_rnd.p);
+  }
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Lay out, allocate and upload everything a batch's launches need.
+int batch_prepare(Batch& b, Context& c) {
+  const int n = int(b.items.size());
+  const long long tile_tex = dither_tile_texels();
+  // tables laid out in b.tables: DitherItem[n], tile offsets[n], then per
+  // format EncodeArgs[n_f] and block offsets[n_f]
+  std::vector<DitherItem> ditems(n);
+  std::vector<long long> toff(n);
+  std::vector<long long> tex_off(n);
+  long long tiles = 0, texels = 0;
+  for (int i = 0; i < n; ++i) {
+    const s2tc_image& im = b.items[i];
+    const long long npx = (long long)im.width * im.height;
+    tex_off[i] = texels;
+    texels += (npx + 3) & ~3ll;  // 16-byte aligned texel rows of each image
+    toff[i] = tiles;
+    tiles += (npx + tile_tex - 1) / tile_tex;
+  }
+  if (!b.t565.reserve(size_t(texels) * 4 + 64, "cudaMalloc(batch texels)")) return ST_OUT_OF_MEMORY;
+  for (int i = 0; i < n; ++i) {
+    const s2tc_image& im = b.items[i];
+    const int dxt = format_dxt(im.format);
+    ditems[i] = DitherItem{static_cast<const uint8_t*>(im.src), im.width, im.height, im.srccomps == 3 ? 3 : 4,
+                           alpha_bits(dxt), b.t565.as<uint32_t>() + tex_off[i]};
+  }
+  // per-format encode tables
+  std::vector<EncodeArgs> eargs[3];
+  std::vector<long long> eoff[3];
+  long long etotal[3] = {0, 0, 0};
+  const int per_block_words[3] = {b.opt.nrandom > 0 ? b.opt.nrandom * 3 : 0, b.opt.nrandom > 0 ? b.opt.nrandom * 3 : 0,
+                                  b.opt.nrandom > 0 ? b.opt.nrandom * 4 : 0};
+  long long rand_pos = 0;
+  for (int i = 0; i < n; ++i) {
+    const s2tc_image& im = b.items[i];
+    const int dxt = format_dxt(im.format);
+    EncodeArgs ea{};
+    ea.t565 = b.t565.as<uint32_t>() + tex_off[i];
+    ea.width = im.width;
+    ea.height = im.height;
+    ea.bw = (im.width + 3) / 4;
+    ea.bh = (im.height + 3) / 4;
+    ea.by0 = 0;
+    ea.nby = ea.bh;
+    ea.dst = static_cast<uint8_t*>(im.dst);
+    ea.pitch = im.dst_pitch;
+    const int bs = block_bytes(dxt);
+    ea.aligned = ((reinterpret_cast<uintptr_t>(im.dst) % bs) == 0 && (im.dst_pitch % bs) == 0) ? 1 : 0;
+    ea.nrandom = b.opt.nrandom;
+    ea.prev_a1_first = -1;
+    ea.leftover_out = nullptr;
+    ea.rnd = nullptr;
+    if (b.normal && b.opt.nrandom > 0) {
+      if (im.rand) {
+        ea.rnd = im.rand;
+      } else {
+        ea.rnd = b.rnd.as<uint32_t>() + rand_pos;
+        rand_pos += (long long)ea.bw * ea.bh * per_block_words[dxt];
+      }
+    }
+    eoff[dxt].push_back(etotal[dxt]);
+    etotal[dxt] += (long long)ea.bw * ea.bh;
+    eargs[dxt].push_back(ea);
+  }
+  // upload the tables (pinned staging, copied inside the graph)
+  size_t off = 0;
+  const size_t o_ditems = off;
+  off = align_up(off + sizeof(DitherItem) * n, 16);
+  const size_t o_toff = off;
+  off = align_up(off + sizeof(long long) * n, 16);
+  size_t o_eargs[3], o_eoff[3];
+  for (int d = 0; d < 3; ++d) {
+    o_eargs[d] = off;
+    off = align_up(off + sizeof(EncodeArgs) * eargs[d].size(), 16);
+    o_eoff[d] = off;
+    off = align_up(off + sizeof(long long) * eoff[d].size(), 16);
+  }
+  if (!b.tables.reserve(off + 16, "cudaMalloc(batch tables)")) return ST_OUT_OF_MEMORY;
+  std::vector<unsigned char> host(off + 16, 0);
+  std::memcpy(host.data() + o_ditems, ditems.data(), sizeof(DitherItem) * n);
+  std::memcpy(host.data() + o_toff, toff.data(), sizeof(long long) * n);
+  for (int d = 0; d < 3; ++d) {
+    if (!eargs[d].empty()) std::memcpy(host.data() + o_eargs[d], eargs[d].data(), sizeof(EncodeArgs) * eargs[d].size());
+    if (!eoff[d].empty()) std::memcpy(host.data() + o_eoff[d], eoff[d].data(), sizeof(long long) * eoff[d].size());
+  }
+  // the tables are constant for the plan: upload them now, outside the graph
+  if (!cuda_ok(cudaMemcpy(b.tables.p, host.data(), off, cudaMemcpyHostToDevice), "batch table upload"))
+    return ST_CUDA_ERROR;
+  unsigned char* tb = b.tables.as<unsigned char>();
+
+  // scratch: SIMPLE/NONE tiles, or one Floyd-Steinberg area per image
+  std::vector<size_t> fs_off(n, 0);
+  size_t scratch = dither_batch_scratch_bytes(tiles);
+  if (b.opt.dither == DI_FLOYDSTEINBERG) {
+    scratch = 0;
+    for (int i = 0; i < n; ++i) {
+      fs_off[i] = scratch;
+      scratch = align_up(scratch + dither_fs_scratch_bytes(b.items[i].width, b.items[i].height), 256);
+    }
+  }
+  if (!b.scratch.reserve(scratch + 256, "cudaMalloc(batch scratch)")) return ST_OUT_OF_MEMORY;
+
+  // --- launch descriptors
+  b.fs_items.clear();
+  b.fs_off = fs_off;
+  if (b.opt.dither == DI_FLOYDSTEINBERG) {
+    for (int i = 0; i < n; ++i) {
+      DitherArgs da{};
+      da.src = ditems[i].src;
+      da.width = ditems[i].width;
+      da.height = ditems[i].height;
+      da.srccomps = ditems[i].srccomps;
+      da.alphabits = ditems[i].alphabits;
+      da.dst = ditems[i].dst;
+      da.error = c.err.as<int>();
+      b.fs_items.push_back(da);
+    }
+  } else {
+    b.dwork = DitherWork{};
+    b.dwork.items = reinterpret_cast<const DitherItem*>(tb + o_ditems);
+    b.dwork.tile_offsets = reinterpret_cast<const long long*>(tb + o_toff);
+    b.dwork.nitems = n;
+    b.dwork.total_tiles = tiles;
+    b.dwork.error = c.err.as<int>();
+  }
+  for (int d = 0; d < 3; ++d) {
+    b.has_fmt[d] = !eargs[d].empty();
+    if (!b.has_fmt[d]) continue;
+    EncodeWork& w = b.ework[d];
+    w = EncodeWork{};
+    w.items = reinterpret_cast<const EncodeArgs*>(tb + o_eargs[d]);
+    w.offsets = reinterpret_cast<const long long*>(tb + o_eoff[d]);
+    w.nitems = int(eargs[d].size());
+    w.total = etotal[d];
+    w.nrandom = b.opt.nrandom;
+  }
+  return ST_OK;
+}
+
+// The launch sequence of a batch on stream `s` (captured once into the graph).
+int batch_launch(Batch& b, cudaStream_t s) {
+  const long long l0 = launches_so_far();
+  if (b.host_rand_words > 0) {
+    if (!cuda_ok(cudaMemcpyAsync(b.rnd.p, b.host_rnd.p, size_t(b.host_rand_words) * 4, cudaMemcpyHostToDevice, s),
+                 "batch rand upload"))
+      return ST_CUDA_ERROR;
+  }
+  if (b.opt.dither == DI_FLOYDSTEINBERG) {
+    for (size_t i = 0; i < b.fs_items.size(); ++i)
+      if (!cuda_ok(launch_dither(b.fs_items[i], DI_FLOYDSTEINBERG, b.scratch.as<uint8_t>() + b.fs_off[i], s),
+                   "batch dither"))
+        return ST_CUDA_ERROR;
+  } else {
+    if (!cuda_ok(launch_dither_batch(b.dwork, b.opt.dither, b.scratch.as<uint8_t>(), s), "batch dither"))
+      return ST_CUDA_ERROR;
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (!b.has_fmt[d]) continue;
+    if (!cuda_ok(launch_encode(b.ework[d], d, b.opt.metric, b.normal, b.opt.refine, s), "batch encode"))
+      return ST_CUDA_ERROR;
+  }
+  b.kernels = int(launches_so_far() - l0);
+  return ST_OK;
+}
+
+}  // namespace
+}  // namespace s2tc
+
+struct s2tc_batch {
+  s2tc::Batch impl;
+};
+
+namespace s2tc {
+namespace {
+
 // ----------------------------------------------------------- block shims
 
 // Leftover second alpha endpoint of the previous shim call on this thread,
@@ -450,6 +663,7 @@ void fetch_texel(int dxt, bool rgba_dxt1, int stride, const unsigned char* data,
 }  // namespace s2tc
 
 using s2tc::Context;
+using s2tc::count_launches;
 using s2tc::DitherArgs;
 using s2tc::check_error_flag;
 using s2tc::compress_device_locked;
@@ -617,6 +831,114 @@ int s2tc_gpu_stage_ms(float* dither_ms, float* encode_ms, long long* calls) {
 }
 
 long long s2tc_gpu_kernel_launches(void) { return s2tc::launches_so_far(); }
+
+int s2tc_batch_create(s2tc_batch** out, const s2tc_image* items, int count, const s2tc_options* opt) {
+  if (!out || !opt || count < 0 || (count > 0 && !items)) {
+    set_error("bad argument");
+    return S2TC_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  s2tc_options o = normalise(*opt);
+  for (int i = 0; i < count; ++i) {
+    const s2tc_image& im = items[i];
+    if (format_dxt(im.format) < 0) {
+      set_error("bad destination format in batch item " + std::to_string(i));
+      return S2TC_ERR_FORMAT;
+    }
+    if (im.width < 0 || im.height < 0 ||
+        (im.width > 0 && im.height > 0 &&
+         (!im.src || !im.dst || im.dst_pitch < (long long)((im.width + 3) / 4) * s2tc::block_bytes(format_dxt(im.format))))) {
+      set_error("bad batch item " + std::to_string(i));
+      return S2TC_ERR_ARGUMENT;
+    }
+  }
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  s2tc_batch* h = new s2tc_batch();
+  s2tc::Batch& b = h->impl;
+  b.opt = o;
+  b.normal = o.nrandom >= 0 || o.metric == s2tc::CD_NORMALMAP;
+  for (int i = 0; i < count; ++i)
+    if (items[i].width > 0 && items[i].height > 0) b.items.push_back(items[i]);
+  // rand words replayed on the host for images without their own stream
+  if (b.normal && o.nrandom > 0) {
+    for (const s2tc_image& im : b.items) {
+      const long long words =
+          (long long)((im.width + 3) / 4) * ((im.height + 3) / 4) * o.nrandom * (format_dxt(im.format) == s2tc::DXT5 ? 4 : 3);
+      b.rand_words.push_back(im.rand ? 0 : words);
+      b.host_rand_words += im.rand ? 0 : words;
+    }
+    if (b.host_rand_words > 0) {
+      if (!b.rnd.reserve(size_t(b.host_rand_words) * 4, "cudaMalloc(batch rand)") ||
+          !b.host_rnd.reserve(size_t(b.host_rand_words) * 4, "cudaMallocHost(batch rand)")) {
+        delete h;
+        return S2TC_ERR_NOMEM;
+      }
+    }
+  }
+  int st = S2TC_OK;
+  if (!cuda_ok(cudaStreamCreateWithFlags(&b.capture, cudaStreamNonBlocking), "cudaStreamCreate") ||
+      !cuda_ok(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming), "cudaEventCreate")) {
+    delete h;
+    return S2TC_ERR_CUDA;
+  }
+  if (!b.items.empty()) {
+    st = s2tc::batch_prepare(b, c);
+    if (st != S2TC_OK) {
+      delete h;
+      return st;
+    }
+    if (!cuda_ok(cudaStreamBeginCapture(b.capture, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture")) {
+      delete h;
+      return S2TC_ERR_CUDA;
+    }
+    st = s2tc::batch_launch(b, b.capture);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b.capture, &g);
+    b.graph = g;
+    if (st == S2TC_OK && !cuda_ok(e, "cudaStreamEndCapture")) st = S2TC_ERR_CUDA;
+    if (st == S2TC_OK && !cuda_ok(cudaGraphInstantiate(&b.exec, b.graph, 0), "cudaGraphInstantiate"))
+      st = S2TC_ERR_CUDA;
+  }
+  if (st != S2TC_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return S2TC_OK;
+}
+
+int s2tc_batch_run(s2tc_batch* h, void* stream) {
+  if (!h) {
+    set_error("null batch");
+    return S2TC_ERR_ARGUMENT;
+  }
+  s2tc::Batch& b = h->impl;
+  if (b.items.empty()) return S2TC_OK;
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+  // a previous run of this plan must be done with the staging and scratch
+  if (!cuda_ok(cudaEventSynchronize(b.done), "cudaEventSynchronize")) return S2TC_ERR_CUDA;
+  if (b.host_rand_words > 0) {
+    // libc rand() in image order, exactly as one tx_compress_dxtn call per image would draw it
+    unsigned int* hr = static_cast<unsigned int*>(b.host_rnd.p);
+    for (long long i = 0; i < b.host_rand_words; ++i) hr[i] = unsigned(std::rand());
+  }
+  if (!cuda_ok(cudaGraphLaunch(b.exec, s), "cudaGraphLaunch")) return S2TC_ERR_CUDA;
+  s2tc::count_launches(b.kernels);
+  if (!cuda_ok(cudaEventRecord(b.done, s), "cudaEventRecord")) return S2TC_ERR_CUDA;
+  return S2TC_OK;
+}
+
+void s2tc_batch_destroy(s2tc_batch* h) {
+  if (!h) return;
+  cudaEventSynchronize(h->impl.done);
+  delete h;
+}
+
+int s2tc_batch_kernels(const s2tc_batch* h) { return h ? h->impl.kernels : 0; }
 
 const char* s2tc_last_error(void) { return s2tc::g_last_error.c_str(); }
 

@@ -204,40 +204,42 @@ __device__ __forceinline__ void load4(const uint8_t* __restrict__ src, long long
   }
 }
 
-template <int SC, int AK>
-__global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
-  __shared__ __align__(16) uint8_t tbl[2][kThreads][kRec];
-  __shared__ uint4 s_c3[256], s_c2[256];
-  __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_carry;
+// Shared memory of one SIMPLE-dither tile.
+struct TileSmem {
+  uint8_t tbl[2][kThreads][kRec];
+  uint4 c3[256], c2[256];
+  uint32_t carry;
+};
 
+// One SIMPLE-dither tile: texels [tile_in_image * kTile, +kTile) of `it`,
+// chained through the status words `status[tile - tile_in_image ...]`.
+// `g` is the tile's global index (status / aggregate slot).
+template <int SC, int AK>
+__device__ __forceinline__ void simple_tile(const DitherItem& it, long long tile_in_image, long long g,
+                                            const DitherWork& w, TileSmem& sm) {
   const int t = threadIdx.x;
-  s_c3[t] = swar_const<3>(t);
-  s_c2[t] = swar_const<2>(t);
-  if (t == 0) s_tile = atomicAdd(a.ticket, 1u);
-  __syncthreads();
-  const long long tile = s_tile;
-  const long long npx = (long long)a.width * a.height;
-  const long long p0 = tile * kTile + (long long)t * kSeg;
+  const long long npx = (long long)it.width * it.height;
+  const long long p0 = tile_in_image * kTile + (long long)t * kSeg;
   const int nvalid = int(max(0ll, min((long long)kSeg, npx - p0)));
+  const int alpha_const = (1 << it.alphabits) - 1;
 
   // segment tables: all start states at once, four per word
   uint32_t wr[4] = {0x13121110u, 0x17161514u, 0x1B1A1918u, 0x171E1D1Cu};  // red states 0..14 (+pad)
   uint32_t wb[4] = {0x13121110u, 0x17161514u, 0x1B1A1918u, 0x171E1D1Cu};  // blue
   uint32_t wg[2] = {0x13121110u, 0x13161514u};                            // green states 0..6 (+pad)
   int asum = 0;
-  uint8_t* mine = tbl[0][t];
+  uint8_t* mine = sm.tbl[0][t];
   if (AK == 4) {
     for (int s = 0; s < QChan<4>::kStates; ++s) mine[kOffA + s] = uint8_t(s);
   }
   for (int k0 = 0; k0 < nvalid; k0 += 4) {
     uint32_t px[4];
-    load4<SC>(a.src, p0 + k0, npx, px);
+    load4<SC>(it.src, p0 + k0, npx, px);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if (k0 + k < nvalid) {
         const uint32_t p = px[k];
-        const uint4 cr = s_c3[p & 0xFF], cg = s_c2[(p >> 8) & 0xFF], cb = s_c3[(p >> 16) & 0xFF];
+        const uint4 cr = sm.c3[p & 0xFF], cg = sm.c2[(p >> 8) & 0xFF], cb = sm.c3[(p >> 16) & 0xFF];
 #pragma unroll
         for (int i = 0; i < 4; ++i) wr[i] = swar_step<3>(wr[i], cr);
 #pragma unroll
@@ -266,30 +268,32 @@ __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
   // inclusive scan of the tables across the CTA
   int cur = 0;
   for (int off = 1; off < kThreads; off <<= 1) {
-    if (t >= off) compose<AK>(tbl[cur][t - off], tbl[cur][t], tbl[cur ^ 1][t]);
+    if (t >= off) compose<AK>(sm.tbl[cur][t - off], sm.tbl[cur][t], sm.tbl[cur ^ 1][t]);
     else
-      for (int i = 0; i < kRec; ++i) tbl[cur ^ 1][t][i] = tbl[cur][t][i];
+      for (int i = 0; i < kRec; ++i) sm.tbl[cur ^ 1][t][i] = sm.tbl[cur][t][i];
     __syncthreads();
     cur ^= 1;
   }
 
-  // chain the tiles: publish, look back, publish the inclusive state
+  // chain the image's tiles: publish, look back, publish the inclusive state
   if (t == 0) {
-    const uint8_t* agg = tbl[cur][kThreads - 1];
-    Status st(a.status[tile]);
+    const uint8_t* agg = sm.tbl[cur][kThreads - 1];
+    Status st(w.status[g]);
     uint32_t carry = initial_state<AK>();
-    if (tile == 0) {
+    if (tile_in_image == 0) {
       st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
     } else {
-      uint8_t* gagg = a.aggs + tile * kRec;
+      uint8_t* gagg = w.aggs + g * kRec;
       for (int i = 0; i < kRec; ++i) gagg[i] = agg[i];
       st.store(kAggReady, cuda::memory_order_release);
-      // acc: state at the end of tile k -> state at the start of this tile
+      // acc: state at the end of tile k -> state at the start of this tile;
+      // the image's first tile always publishes its inclusive state, so the
+      // walk never leaves the image
       uint8_t acc[kRec];
       identity<AK>(acc);
-      long long k = tile - 1;
+      long long k = g - 1;
       for (;;) {
-        Status sk(a.status[k]);
+        Status sk(w.status[k]);
         unsigned long long v = sk.load(cuda::memory_order_acquire);
         int spins = 0;
         while ((v >> 32) == 0 && spins < kSpinLimit) {
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
           ++spins;
         }
         if ((v >> 32) == 0) {
-          atomicExch(a.error, 1);
+          atomicExch(w.error, 1);
           break;
         }
         if ((v >> 32) == 2) {
@@ -307,26 +311,26 @@ __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
         }
         // acc := agg[k] then acc
         uint8_t tmp[kRec];
-        compose<AK>(a.aggs + k * kRec, acc, tmp);
+        compose<AK>(w.aggs + k * kRec, acc, tmp);
         for (int i = 0; i < kRec; ++i) acc[i] = tmp[i];
         --k;
       }
       st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
     }
-    s_carry = carry;
+    sm.carry = carry;
   }
   __syncthreads();
 
   // replay the segment from its exact start state
-  const uint32_t start = t == 0 ? s_carry : apply<AK>(tbl[cur][t - 1], s_carry);
+  const uint32_t start = t == 0 ? sm.carry : apply<AK>(sm.tbl[cur][t - 1], sm.carry);
   int dr = int(start & 0xFF) - QChan<3>::kOff;
   int dg = int((start >> 8) & 0xFF) - QChan<2>::kOff;
   int db = int((start >> 16) & 0xFF) - QChan<3>::kOff;
   int da = AK == 4 ? int(start >> 24) - QChan<4>::kOff : int(start >> 24) - 127;
-  uint32_t* o = a.dst + p0;
+  uint32_t* o = it.dst + p0;
   for (int k0 = 0; k0 < nvalid; k0 += 4) {
     uint32_t px[4], out[4];
-    load4<SC>(a.src, p0 + k0, npx, px);
+    load4<SC>(it.src, p0 + k0, npx, px);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const uint32_t p = px[k];
@@ -343,45 +347,68 @@ __global__ void __launch_bounds__(kThreads) k_dither_simple(DitherArgs a) {
       } else if (AK == 8) {
         qa = uint32_t(chan_of(p, 3));
       } else {
-        qa = uint32_t(a.alpha_const);
+        qa = uint32_t(alpha_const);
       }
       out[k] = q | (qa << 24);
     }
-    if (k0 + 4 <= nvalid) {
+    if (k0 + 4 <= nvalid && (reinterpret_cast<uintptr_t>(o + k0) & 15) == 0) {
       *reinterpret_cast<uint4*>(o + k0) = make_uint4(out[0], out[1], out[2], out[3]);
     } else {
-      for (int k = 0; k < nvalid - k0; ++k) o[k0 + k] = out[k];
+      for (int k = 0; k < min(4, nvalid - k0); ++k) o[k0 + k] = out[k];
     }
   }
 }
 
-// DITHER_NONE (s2tc_algorithm.cpp:1269-1305): plain truncation.
-template <int SC>
-__global__ void __launch_bounds__(256) k_dither_none(DitherArgs a) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long npx = (long long)a.width * a.height;
-  if (p >= npx) return;
-  const uint8_t* s = a.src + p * SC;
-  uint32_t r = s[0] >> 3, g = s[1] >> 2, b = s[2] >> 3;
-  uint32_t al = SC == 4 ? uint32_t(s[3] >> (8 - a.alphabits)) : uint32_t(a.alpha_const);
-  a.dst[p] = r | (g << 8) | (b << 16) | (al << 24);
+// Image of global tile g: the last image whose first tile is <= g.
+__device__ __forceinline__ int tile_item(const DitherWork& w, long long g) {
+  if (!w.items) return 0;
+  int lo = 0, hi = w.nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(w.tile_offsets + mid) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
-template <int SC>
-cudaError_t launch_simple(const DitherArgs& a, cudaStream_t s) {
-  const long long npx = (long long)a.width * a.height;
-  const unsigned grid = unsigned((npx + kTile - 1) / kTile);
-  count_launches(1);
-  if (SC == 3) {
-    k_dither_simple<SC, 0><<<grid, kThreads, 0, s>>>(a);
-  } else if (a.alphabits == 1) {
-    k_dither_simple<SC, 1><<<grid, kThreads, 0, s>>>(a);
-  } else if (a.alphabits == 4) {
-    k_dither_simple<SC, 4><<<grid, kThreads, 0, s>>>(a);
-  } else {
-    k_dither_simple<SC, 8><<<grid, kThreads, 0, s>>>(a);
+// DITHER_SIMPLE over every tile of every image of the work list.  Tiles take
+// tickets in launch order, so a tile only ever waits on tiles that started
+// before it.
+__global__ void __launch_bounds__(kThreads) k_dither_simple(DitherWork w) {
+  __shared__ TileSmem sm;
+  __shared__ unsigned int s_ticket;
+  const int t = threadIdx.x;
+  sm.c3[t] = swar_const<3>(t);
+  sm.c2[t] = swar_const<2>(t);
+  if (t == 0) s_ticket = atomicAdd(w.ticket, 1u);
+  __syncthreads();
+  const long long g = s_ticket;
+  if (g >= w.total_tiles) return;
+  const int item = tile_item(w, g);
+  const DitherItem it = w.items ? w.items[item] : w.single;
+  const long long lt = w.items ? g - __ldg(w.tile_offsets + item) : g;
+  if (it.srccomps == 3) simple_tile<3, 0>(it, lt, g, w, sm);
+  else if (it.alphabits == 1) simple_tile<4, 1>(it, lt, g, w, sm);
+  else if (it.alphabits == 4) simple_tile<4, 4>(it, lt, g, w, sm);
+  else simple_tile<4, 8>(it, lt, g, w, sm);
+}
+
+// DITHER_NONE (s2tc_algorithm.cpp:1269-1305): plain truncation, one tile per CTA.
+__global__ void __launch_bounds__(kThreads) k_dither_none(DitherWork w) {
+  const long long g = blockIdx.x;
+  if (g >= w.total_tiles) return;
+  const int item = tile_item(w, g);
+  const DitherItem it = w.items ? w.items[item] : w.single;
+  const long long npx = (long long)it.width * it.height;
+  const long long base = (w.items ? g - __ldg(w.tile_offsets + item) : g) * kTile;
+  const int sc = it.srccomps == 3 ? 3 : 4;
+  const uint32_t ac = uint32_t((1 << it.alphabits) - 1);
+  for (long long p = base + threadIdx.x; p < min(npx, base + kTile); p += kThreads) {
+    const uint8_t* s = it.src + p * sc;
+    const uint32_t r = s[0] >> 3, gg = s[1] >> 2, b = s[2] >> 3;
+    const uint32_t al = sc == 4 ? uint32_t(s[3] >> (8 - it.alphabits)) : ac;
+    it.dst[p] = r | (gg << 8) | (b << 16) | (al << 24);
   }
-  return cudaGetLastError();
 }
 
 std::atomic<long long> g_launches{0};
@@ -391,10 +418,33 @@ std::atomic<long long> g_launches{0};
 void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
-size_t dither_scratch_bytes(long long npx) {
-  const long long tiles = (npx + kTile - 1) / kTile;
-  // status words, aggregate tables, ticket + error flag
+long long dither_tile_texels() { return kTile; }
+
+size_t dither_batch_scratch_bytes(long long tiles) {
+  // status words, aggregate tables, ticket (plus alignment slack)
   return size_t(tiles) * (sizeof(unsigned long long) + kRec) + 256;
+}
+
+size_t dither_scratch_bytes(long long npx) { return dither_batch_scratch_bytes((npx + kTile - 1) / kTile); }
+
+cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cudaStream_t s) {
+  if (w.total_tiles <= 0) return cudaSuccess;
+  if (dither == DI_NONE) {
+    count_launches(1);
+    k_dither_none<<<unsigned(w.total_tiles), kThreads, 0, s>>>(w);
+    return cudaGetLastError();
+  }
+  w.status = reinterpret_cast<unsigned long long*>(scratch);
+  w.aggs = scratch + w.total_tiles * sizeof(unsigned long long);
+  uintptr_t tk = reinterpret_cast<uintptr_t>(w.aggs + w.total_tiles * kRec);
+  w.ticket = reinterpret_cast<unsigned int*>((tk + 15) & ~uintptr_t(15));
+  cudaError_t e = cudaMemsetAsync(w.status, 0, w.total_tiles * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  count_launches(1);
+  k_dither_simple<<<unsigned(w.total_tiles), kThreads, 0, s>>>(w);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream_t s) {
@@ -402,25 +452,14 @@ cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream
   if (npx <= 0) return cudaSuccess;
   a.alpha_const = (1 << a.alphabits) - 1;
   if (dither == DI_FLOYDSTEINBERG) return launch_dither_fs(a, scratch, s);
-  if (dither == DI_NONE) {
-    const unsigned grid = unsigned((npx + 255) / 256);
-    count_launches(1);
-    if (a.srccomps == 3) k_dither_none<3><<<grid, 256, 0, s>>>(a);
-    else k_dither_none<4><<<grid, 256, 0, s>>>(a);
-    return cudaGetLastError();
-  }
-  // DI_SIMPLE (DI_FLOYDSTEINBERG is handled by dither_fs.cu)
-  const long long tiles = (npx + kTile - 1) / kTile;
-  a.status = reinterpret_cast<unsigned long long*>(scratch);
-  a.aggs = scratch + tiles * sizeof(unsigned long long);
-  a.ticket = reinterpret_cast<unsigned int*>(a.aggs + tiles * kRec);
-  a.ticket = reinterpret_cast<unsigned int*>((reinterpret_cast<uintptr_t>(a.ticket) + 15) & ~uintptr_t(15));
-  cudaError_t e = cudaMemsetAsync(a.status, 0, tiles * sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned int), s);
-  if (e != cudaSuccess) return e;
-  if (a.srccomps == 3) return launch_simple<3>(a, s);
-  return launch_simple<4>(a, s);
+  DitherWork w{};
+  w.items = nullptr;
+  w.tile_offsets = nullptr;
+  w.nitems = 1;
+  w.single = DitherItem{a.src, a.width, a.height, a.srccomps == 3 ? 3 : 4, a.alphabits, a.dst};
+  w.total_tiles = (npx + kTile - 1) / kTile;
+  w.error = a.error;
+  return launch_dither_batch(w, dither, scratch, s);
 }
 
 }  // namespace s2tc

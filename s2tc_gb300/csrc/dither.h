@@ -25,8 +25,35 @@ struct DitherArgs {
   unsigned int* ticket;
 };
 
-// Scratch bytes that launch_dither needs for an image of `npx` texels.
+// One image of a batched dither launch.
+struct DitherItem {
+  const uint8_t* src;
+  int width, height, srccomps, alphabits;
+  uint32_t* dst;
+};
+
+// Batched DITHER_NONE / DITHER_SIMPLE over many images: the images' 16384-texel
+// tiles are numbered consecutively (`tile_offsets[i]` = first tile of image i,
+// images with no texels left out) and every CTA takes one tile.
+struct DitherWork {
+  const DitherItem* items;      // device array, or null for the single image below
+  const long long* tile_offsets;  // device array, nitems entries
+  int nitems;
+  DitherItem single;
+  long long total_tiles;
+  int* error;
+  unsigned long long* status;   // total_tiles status words (zeroed before launch)
+  uint8_t* aggs;                // total_tiles aggregate tables
+  unsigned int* ticket;         // zeroed before launch
+};
+
+// Texels per tile of the batched/SIMPLE dither kernels.
+long long dither_tile_texels();
+
+// Scratch bytes that launch_dither needs for an image of `npx` texels, and
+// that launch_dither_batch needs for `tiles` tiles in total.
 size_t dither_scratch_bytes(long long npx);
+size_t dither_batch_scratch_bytes(long long tiles);
 size_t dither_fs_scratch_bytes(int width, int height);
 
 // Runs the reference's rgb565_image for `dither` (DI_NONE, DI_SIMPLE or
@@ -34,5 +61,8 @@ size_t dither_fs_scratch_bytes(int width, int height);
 // scratch sizes above.
 cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream_t s);
 cudaError_t launch_dither_fs(DitherArgs a, uint8_t* scratch, cudaStream_t s);
+// Batched NONE / SIMPLE dither (`dither` DI_NONE or DI_SIMPLE); `w.status`,
+// `w.aggs` and `w.ticket` point into `scratch` once this returns.
+cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cudaStream_t s);
 
 }  // namespace s2tc

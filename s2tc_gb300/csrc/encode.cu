@@ -414,15 +414,35 @@ __device__ __forceinline__ void store_block(const EncodeArgs& a, int dxt, int bx
   }
 }
 
+// The image and its block-within-launch index for global work item g.
+__device__ __forceinline__ bool resolve(const EncodeWork& w, long long g, EncodeArgs& a, long long& bl) {
+  if (g >= w.total) return false;
+  if (!w.items) {
+    a = w.single;
+    bl = g;
+    return true;
+  }
+  int lo = 0, hi = w.nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(w.offsets + mid) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  a = w.items[lo];
+  bl = g - __ldg(w.offsets + lo);
+  return true;
+}
+
 // Full blocks of the all-texels mode without random candidates.
 #ifndef S2TC_FULL16_MINBLOCKS
 #define S2TC_FULL16_MINBLOCKS 1
 #endif
 template <int DXT, int REFINE>
-__global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encode_full16(EncodeArgs a) {
+__global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encode_full16(EncodeWork w) {
   __shared__ Scratch16 sc;
-  const long long bl = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (bl >= (long long)a.bw * a.nby) return;
+  EncodeArgs a;
+  long long bl;
+  if (!resolve(w, (long long)blockIdx.x * blockDim.x + threadIdx.x, a, bl)) return;
   const long long b = (long long)a.by0 * a.bw + bl;
   const int by = int(b / a.bw), bx = int(b % a.bw);
   BlockTexels bt;
@@ -437,10 +457,11 @@ __global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encod
 // DXT1 blocks with transparent texels.  In the all-texels mode without random
 // candidates the full blocks are skipped (k_encode_full16 encodes them).
 template <int DXT, bool NORMAL, int REFINE>
-__global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeArgs a) {
+__global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
   __shared__ Scratch16 sc;
-  const long long bl = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // block within this launch
-  if (bl >= (long long)a.bw * a.nby) return;
+  EncodeArgs a;
+  long long bl;  // block within this launch's part of the image
+  if (!resolve(w, (long long)blockIdx.x * blockDim.x + threadIdx.x, a, bl)) return;
   const long long b = (long long)a.by0 * a.bw + bl;                         // block within the image
   const int by = int(b / a.bw), bx = int(b % a.bw);
   BlockTexels bt;
@@ -656,7 +677,7 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
 }
 
 template <int DXT, int REFINE>
-__global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeArgs a, int m) {
+__global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeWork w, int m) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const RandLayout L = rand_layout(m);
@@ -666,11 +687,14 @@ __global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeArgs a, i
   uint8_t* sA = base + L.a;
   int32_t* sD = reinterpret_cast<int32_t*>(base + L.d);
   uint8_t* sE = base + L.e;
-  const int nrandom = a.nrandom;
+  const int nrandom = w.nrandom;
   const int stride = DXT == DXT5 ? 4 : 3;
-  const long long nb = (long long)a.bw * a.nby;
+  const long long nb = w.total;
 
-  for (long long bl = (long long)blockIdx.x * kRandWarps + warp; bl < nb; bl += (long long)gridDim.x * kRandWarps) {
+  for (long long g = (long long)blockIdx.x * kRandWarps + warp; g < nb; g += (long long)gridDim.x * kRandWarps) {
+    EncodeArgs a;
+    long long bl;
+    resolve(w, g, a, bl);
     const long long b = (long long)a.by0 * a.bw + bl;
     const int by = int(b / a.bw), bx = int(b % a.bw);
     const int bw_ = min(4, a.width - bx * 4), bh_ = min(4, a.height - by * 4);
@@ -879,8 +903,8 @@ size_t rand_smem_bytes(int m) {
 }
 
 template <int DXT, bool NORMAL>
-cudaError_t launch_r(const EncodeArgs& a, int refine, cudaStream_t s) {
-  const long long nb = (long long)a.bw * a.nby;
+cudaError_t launch_r(const EncodeWork& a, int refine, cudaStream_t s) {
+  const long long nb = a.total;
   if (nb == 0) return cudaSuccess;
   const int threads = kThreadsPerCta;
   const unsigned grid = unsigned((nb + threads - 1) / threads);
@@ -928,7 +952,7 @@ cudaError_t launch_r(const EncodeArgs& a, int refine, cudaStream_t s) {
 }
 
 template <int DXT>
-cudaError_t launch_d(const EncodeArgs& a, bool normal, int refine, cudaStream_t s) {
+cudaError_t launch_d(const EncodeWork& a, bool normal, int refine, cudaStream_t s) {
   // NORMALMAP never uses the quick selection (s2tc_algorithm.cpp:1127-1143)
   if (normal || kMetric == CD_NORMALMAP) return launch_r<DXT, true>(a, refine, s);
   return launch_r<DXT, (kMetric == CD_NORMALMAP)>(a, refine, s);
@@ -939,7 +963,7 @@ cudaError_t launch_d(const EncodeArgs& a, bool normal, int refine, cudaStream_t 
 #define S2TC_CAT2(a, b) a##b
 #define S2TC_CAT(a, b) S2TC_CAT2(a, b)
 
-cudaError_t S2TC_CAT(launch_encode_m, S2TC_METRIC)(const EncodeArgs& a, int dxt, bool normal, int refine,
+cudaError_t S2TC_CAT(launch_encode_m, S2TC_METRIC)(const EncodeWork& a, int dxt, bool normal, int refine,
                                                    cudaStream_t s) {
   switch (dxt) {
     case DXT1: return launch_d<DXT1>(a, normal, refine, s);

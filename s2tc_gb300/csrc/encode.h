@@ -22,29 +22,55 @@ struct EncodeArgs {
   int* leftover_out;     // if set, receives the last block's leftover alpha endpoint
 };
 
-cudaError_t launch_encode_m0(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m1(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m2(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m3(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m4(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m5(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m6(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
-cudaError_t launch_encode_m7(const EncodeArgs&, int dxt, bool normal, int refine, cudaStream_t);
+// Blocks to encode: one image (`single`, items == null) or many images of the
+// same format whose blocks are numbered consecutively (`offsets[i]` = first
+// block of image i; every image has at least one block).  All images share
+// nrandom (the knobs of a launch are uniform).
+struct EncodeWork {
+  const EncodeArgs* items;   // device array, or null
+  const long long* offsets;  // device array, nitems entries
+  int nitems;
+  long long total;           // blocks in all images
+  int nrandom;               // S2TC_RANDOM_COLORS of every image
+  EncodeArgs single;
+};
+
+cudaError_t launch_encode_m0(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m1(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m2(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m3(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m4(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m5(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m6(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
+cudaError_t launch_encode_m7(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
 
 // Dispatch on the metric; `normal` selects the all-candidates search
 // (nrandom >= 0), which NORMALMAP always uses.
-inline cudaError_t launch_encode(const EncodeArgs& a, int dxt, int metric, bool normal, int refine,
+inline cudaError_t launch_encode(const EncodeWork& w, int dxt, int metric, bool normal, int refine,
                                  cudaStream_t s) {
   switch (metric) {
-    case 0: return launch_encode_m0(a, dxt, normal, refine, s);
-    case 1: return launch_encode_m1(a, dxt, normal, refine, s);
-    case 2: return launch_encode_m2(a, dxt, normal, refine, s);
-    case 3: return launch_encode_m3(a, dxt, normal, refine, s);
-    case 4: return launch_encode_m4(a, dxt, normal, refine, s);
-    case 6: return launch_encode_m6(a, dxt, normal, refine, s);
-    case 7: return launch_encode_m7(a, dxt, normal, refine, s);
-    default: return launch_encode_m5(a, dxt, normal, refine, s);
+    case 0: return launch_encode_m0(w, dxt, normal, refine, s);
+    case 1: return launch_encode_m1(w, dxt, normal, refine, s);
+    case 2: return launch_encode_m2(w, dxt, normal, refine, s);
+    case 3: return launch_encode_m3(w, dxt, normal, refine, s);
+    case 4: return launch_encode_m4(w, dxt, normal, refine, s);
+    case 6: return launch_encode_m6(w, dxt, normal, refine, s);
+    case 7: return launch_encode_m7(w, dxt, normal, refine, s);
+    default: return launch_encode_m5(w, dxt, normal, refine, s);
   }
+}
+
+// One image: block rows [a.by0, a.by0 + a.nby).
+inline cudaError_t launch_encode(const EncodeArgs& a, int dxt, int metric, bool normal, int refine,
+                                 cudaStream_t s) {
+  EncodeWork w{};
+  w.items = nullptr;
+  w.offsets = nullptr;
+  w.nitems = 1;
+  w.total = (long long)a.bw * a.nby;
+  w.nrandom = a.nrandom;
+  w.single = a;
+  return launch_encode(w, dxt, metric, normal, refine, s);
 }
 
 }  // namespace s2tc

@@ -226,3 +226,70 @@ def test_mip_chains(lib, oracle):
             a = gpu_compress(t["srccomps"], w, h, lvl.reshape(-1), t["fmt"], 1, 5, 64, 1, seed=seed)
             b = oracle.compress(t["srccomps"], w, h, lvl.reshape(-1), t["fmt"], 1, 5, 64, 1, seed=seed)
             assert np.array_equal(a, b), (w, h, t["fmt"], t["srccomps"])
+
+
+def _batch_vs_single(torch, textures, opt, seed, stream=None):
+    """Encode every level of every texture as one batch and one by one through
+    tx_compress_dxtn (same rand() stream order); return both outputs."""
+    images, refs = [], []
+    for t in textures:
+        for lvl in t["levels"]:
+            h, w = lvl.shape[:2]
+            n = s2.compressed_size(w, h, t["fmt"])
+            images.append({"src": torch.from_numpy(lvl.reshape(-1).copy()).cuda(), "width": w, "height": h,
+                           "srccomps": t["srccomps"], "format": t["fmt"],
+                           "dst": torch.full((n,), 0xA5, dtype=torch.uint8, device="cuda")})
+    b = s2.Batch(images, opt)
+    pyoracle.srand(seed)
+    b.run(stream)
+    s2.gpu_synchronize(stream)
+    got = [im["dst"].cpu().numpy() for im in images]
+    s2.set_env(opt.dither, opt.metric, opt.nrandom, opt.refine)
+    pyoracle.srand(seed)
+    for t in textures:
+        for lvl in t["levels"]:
+            h, w = lvl.shape[:2]
+            refs.append(s2.tx_compress_dxtn(t["srccomps"], w, h, lvl.reshape(-1), t["fmt"]))
+    b.close()
+    return got, refs
+
+
+@pytest.mark.parametrize("dither", [0, 1, 2])
+def test_batch_mip_chains(lib, dither):
+    """One graph launch for uneven mip chains (down to 1x1, with 2x2 and 3xN
+    edge levels), mixed formats and component counts, against one
+    tx_compress_dxtn call per level."""
+    torch = pytest.importorskip("torch")
+    tex = workloads.mip_textures(31 + dither, count=9, lo=3, hi=150)
+    for opt in (s2.options(dither, s2.WAVG, 8, 1), s2.options(dither, s2.SRGB_MIXED, 0, 2),
+                s2.options(dither, s2.W0AVG, -1, 0)):
+        got, refs = _batch_vs_single(torch, tex, opt, 77)
+        for g, r in zip(got, refs):
+            assert np.array_equal(g, r)
+
+
+def test_batch_repeated_runs(lib):
+    """A plan runs again with new pixel contents and gives fresh results."""
+    torch = pytest.importorskip("torch")
+    tex = workloads.mip_textures(5, count=4, lo=8, hi=64)
+    images = []
+    for t in tex:
+        lvl = t["levels"][0]
+        h, w = lvl.shape[:2]
+        images.append({"src": torch.from_numpy(lvl.reshape(-1).copy()).cuda(), "width": w, "height": h,
+                       "srccomps": t["srccomps"], "format": t["fmt"],
+                       "dst": torch.zeros(s2.compressed_size(w, h, t["fmt"]), dtype=torch.uint8, device="cuda")})
+    opt = s2.options(1, s2.SRGB, 0, 2)
+    b = s2.Batch(images, opt)
+    s2.set_env(1, s2.SRGB, 0, 2)
+    for rnd in range(3):
+        for im in images:
+            im["src"].copy_(torch.randint(0, 256, im["src"].shape, dtype=torch.uint8))
+        b.run()
+        s2.gpu_synchronize()
+        for im in images:
+            want = s2.tx_compress_dxtn(im["srccomps"], im["width"], im["height"], im["src"].cpu().numpy(),
+                                       im["format"])
+            assert np.array_equal(im["dst"].cpu().numpy(), want)
+    assert b.kernels >= 2
+    b.close()
