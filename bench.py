@@ -55,6 +55,10 @@ WORKLOADS = {
         w=8192, h=8192, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
     "normal_map_2048_dxt1_normalmap_rand64_loop": dict(
         w=2048, h=2048, sc=3, fmt=0x83F1, dither=1, metric=7, nrandom=64, refine=2, gen="normal", seed=4),
+    # 256 textures (log-uniform 4..2048, aspect <= 4:1) with full mip chains,
+    # mixed DXT1/DXT3/DXT5, RGB8/RGBA8: one batched graph launch per step
+    "mip_chains_256_wavg_rand64_always": dict(
+        w=0, h=0, sc=0, fmt=0, dither=1, metric=5, nrandom=64, refine=1, gen="mips", seed=3, count=256),
 }
 DEFAULT_WORKLOAD = "value_noise_4096_dxt5_srgb_mixed_all16_loop"
 FMT_NAMES = {0x83F0: "DXT1(RGB)", 0x83F1: "DXT1", 0x83F2: "DXT3", 0x83F3: "DXT5"}
@@ -82,6 +86,13 @@ def algorithmic_bytes_per_texel(wl: dict) -> float:
 
 def config_dict(wl_name: str, wl: dict) -> dict:
     import s2tc_gb300 as s2
+    if wl["gen"] == "mips":
+        return {"workload": wl_name, "textures": wl["count"], "base_sizes": "log-uniform 4..2048, aspect <= 4:1",
+                "levels": "full mip chains to 1x1", "formats": "DXT1/DXT3/DXT5 by thirds",
+                "srccomps": "3 and 4 alternating", "dither": s2.DITHER_NAMES[wl["dither"]],
+                "colordist": s2.COLORDIST_NAMES[wl["metric"]], "random_colors": wl["nrandom"],
+                "refine": s2.REFINE_NAMES[wl["refine"]],
+                "l2": "the batch's inputs (over 100 MB) and rand words (GBs) exceed the 129 MB L2"}
     return {"workload": wl_name, "width": wl["w"], "height": wl["h"], "srccomps": wl["sc"],
             "format": FMT_NAMES[wl["fmt"]], "dither": s2.DITHER_NAMES[wl["dither"]],
             "colordist": s2.COLORDIST_NAMES[wl["metric"]], "random_colors": wl["nrandom"],
@@ -238,6 +249,139 @@ def cpu_baseline_port(wl_name: str, wl: dict, gpu_out0: np.ndarray | None) -> di
     return res
 
 
+# ------------------------------------------------------------ batch workload
+
+def run_batch_workload(args, wl_name: str, wl: dict) -> None:
+    """Uneven mip chains: the batched graph launch vs one s2tc_gpu_compress
+    per level, both with the same resident rand words."""
+    import torch
+    import s2tc_gb300 as s2
+    from s2tc_gb300 import workloads
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    tex = workloads.mip_textures(wl["seed"], count=wl["count"], lo=4, hi=2048)
+    opt = s2.options(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+    levels = [(t, lvl) for t in tex for lvl in t["levels"]]
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(11)
+    images, host_src, host_rand = [], [], []
+    texels = 0
+    in_bytes = out_bytes = rand_bytes = 0
+    for t, lvl in levels:
+        h, w = lvl.shape[:2]
+        flat = np.ascontiguousarray(lvl.reshape(-1))
+        words = s2.rand_words(w, h, t["fmt"], opt)
+        rw = torch.randint(0, 2**31 - 1, (max(1, words),), dtype=torch.int32, device="cuda", generator=gen)
+        n = s2.compressed_size(w, h, t["fmt"])
+        images.append({"src": torch.from_numpy(flat).cuda(), "width": w, "height": h, "srccomps": t["srccomps"],
+                       "format": t["fmt"], "dst": torch.empty(n, dtype=torch.uint8, device="cuda"), "rand": rw})
+        host_src.append(torch.from_numpy(flat).pin_memory())
+        host_rand.append(rw.cpu().pin_memory())
+        texels += w * h
+        in_bytes += flat.nbytes
+        out_bytes += n
+        rand_bytes += 4 * words
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    batch = s2.Batch(images, opt)
+    ref_out = [torch.empty_like(im["dst"]) for im in images]
+    each_arr = s2.image_array([dict(im, dst=d) for im, d in zip(images, ref_out)])
+
+    def per_image(dsts):
+        # the per-image path, driven from C: one s2tc_gpu_compress per level
+        s2.gpu_compress_each(images, opt, sp, arr=each_arr)
+
+    for _ in range(args.warmup):
+        batch.run(sp)
+        per_image(ref_out)
+    s2.gpu_synchronize(sp)
+    bit_exact = all(torch.equal(im["dst"], r) for im, r in zip(images, ref_out))
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+
+    l0 = s2.kernel_launches()
+    with ClockSampler(0) as clk:
+        t_batch = timed(lambda: batch.run(sp))
+    launches = s2.kernel_launches() - l0
+    t_single = timed(lambda: per_image(ref_out))
+    s2.gpu_synchronize(sp)
+    value = args.steps * texels / t_batch
+    single = args.steps * texels / t_single
+
+    # end to end: pinned host pixels and rand words in, blocks out, batch launch
+    host_out = [torch.empty(im["dst"].numel(), dtype=torch.uint8).pin_memory() for im in images]
+
+    def e2e_step():
+        for im, hs, hr in zip(images, host_src, host_rand):
+            im["src"].copy_(hs, non_blocking=True)
+            im["rand"].copy_(hr, non_blocking=True)
+        batch.run(sp)
+        for im, ho in zip(images, host_out):
+            ho.copy_(im["dst"], non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the CPU port on a bounded sample: the first levels until ~1.5 M texels
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+        oracle = pyoracle.Oracle()
+        sample, sample_tex = [], 0
+        for t, lvl in levels:
+            sample.append((t, lvl))
+            sample_tex += lvl.shape[0] * lvl.shape[1]
+            if sample_tex >= 1_500_000:
+                break
+        pyoracle.srand(1)
+        c0 = time.perf_counter()
+        for t, lvl in sample:
+            h, w = lvl.shape[:2]
+            oracle.compress(t["srccomps"], w, h, lvl.reshape(-1), t["fmt"], wl["dither"], wl["metric"],
+                            wl["nrandom"], wl["refine"])
+        dt = time.perf_counter() - c0
+        cpu = {"value": sample_tex / dt, "unit": "texels/s", "cores": 1, "kind": "port",
+               "sample": f"the first {len(sample)} levels ({sample_tex} texels), single thread ({dt:.2f} s)"}
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    alg = in_bytes + out_bytes
+    achieved = alg / (t_batch / args.steps) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * t_batch / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": dict(config_dict(wl_name, wl), images=len(images), texels=texels),
+            "per_image": {"value": single, "unit": "texels/s", "ms_per_step": 1000 * t_single / args.steps,
+                          "launches_per_step": None},
+            "batched_over_per_image": value / single, "bit_exact_batched_vs_per_image": bit_exact,
+            "e2e": {"value": args.steps * texels / t_e2e, "unit": "texels/s",
+                    "h2d_bytes_per_step": in_bytes + rand_bytes, "d2h_bytes_per_step": out_bytes,
+                    "ms_per_step": 1000 * t_e2e / args.steps},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": "batch step", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "note": "random-candidate search is integer-ALU bound; frac is of the HBM roofline"},
+            "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------- GPU arm
 
 def main() -> None:
@@ -254,7 +398,13 @@ def main() -> None:
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
+        if wl["gen"] == "mips":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times single-image workloads"}))
+            return
         run_reference_arm(args, args.workload, wl)
+        return
+    if wl["gen"] == "mips":
+        run_batch_workload(args, args.workload, wl)
         return
 
     import torch

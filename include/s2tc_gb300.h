@@ -121,6 +121,10 @@ typedef struct s2tc_image {
 	const unsigned int *rand;
 } s2tc_image;
 
+/* Compress each image with its own launches, one after another on `stream`
+ * (the per-image path that batches replace; same bytes). */
+int s2tc_gpu_compress_each(const s2tc_image *items, int count, const s2tc_options *opt, void *stream);
+
 typedef struct s2tc_batch s2tc_batch;
 
 /* Plan a batch: allocates the device scratch and tables for all images and

@@ -114,6 +114,8 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_gpu_stage_ms.restype = c_int
     lib.s2tc_gpu_kernel_launches.argtypes = []
     lib.s2tc_gpu_kernel_launches.restype = c_ll
+    lib.s2tc_gpu_compress_each.argtypes = [ctypes.POINTER(Image), c_int, ctypes.POINTER(Options), vp]
+    lib.s2tc_gpu_compress_each.restype = c_int
     lib.s2tc_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Image), c_int,
                                       ctypes.POINTER(Options)]
     lib.s2tc_batch_create.restype = c_int
@@ -136,7 +138,7 @@ EXPORTED_SYMBOLS = (
     "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5", "rgb565_image",
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
     "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
-    "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run",
+    "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
     "s2tc_batch_kernels", "s2tc_batch_destroy",
     "s2tc_last_error",
 )
@@ -286,6 +288,27 @@ def gpu_compress_noalloc(srccomps: int, width: int, height: int, d_src, destform
                                                 ctypes.byref(opt), rnd_p, stream))
 
 
+def image_array(images):
+    """ctypes array of ``Image`` from dicts (see ``Batch``)."""
+    arr = (Image * max(1, len(images)))()
+    for i, im in enumerate(images):
+        w, h, fmt = int(im["width"]), int(im["height"]), int(im["format"])
+        pitch = im.get("dst_pitch") or ((w + 3) // 4) * block_bytes(fmt)
+        rnd = im.get("rand")
+        arr[i] = Image(_addr(im["src"]), w, h, int(im["srccomps"]), fmt, _addr(im["dst"]), int(pitch),
+                       None if rnd is None else _addr(rnd))
+    return arr
+
+
+def gpu_compress_each(images, opt: Options, stream: int | None = None, arr=None) -> None:
+    """``s2tc_gpu_compress_each``: one image at a time, each with its own
+    launches (pass a prebuilt ``image_array`` as ``arr`` to skip conversion)."""
+    arr = arr if arr is not None else image_array(images)
+    st = load().s2tc_gpu_compress_each(arr, len(images), ctypes.byref(opt), stream)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_compress_each failed ({st}): {last_error()}")
+
+
 class Batch:
     """A planned batch (``s2tc_batch_create``): images of uneven sizes and
     mixed formats encoded by one CUDA-graph launch per ``run``.
@@ -295,15 +318,8 @@ class Batch:
     pointers)."""
 
     def __init__(self, images, opt: Options):
-        arr = (Image * max(1, len(images)))()
-        self._keep = []
-        for i, im in enumerate(images):
-            w, h, fmt = int(im["width"]), int(im["height"]), int(im["format"])
-            pitch = im.get("dst_pitch") or ((w + 3) // 4) * block_bytes(fmt)
-            rnd = im.get("rand")
-            arr[i] = Image(_addr(im["src"]), w, h, int(im["srccomps"]), fmt, _addr(im["dst"]), int(pitch),
-                           None if rnd is None else _addr(rnd))
-            self._keep.append(im)
+        arr = image_array(images)
+        self._keep = list(images)
         self._opt = opt
         h = ctypes.c_void_p()
         st = load().s2tc_batch_create(ctypes.byref(h), arr, len(images), ctypes.byref(opt))

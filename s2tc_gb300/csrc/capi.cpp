@@ -832,6 +832,31 @@ int s2tc_gpu_stage_ms(float* dither_ms, float* encode_ms, long long* calls) {
 
 long long s2tc_gpu_kernel_launches(void) { return s2tc::launches_so_far(); }
 
+int s2tc_gpu_compress_each(const s2tc_image* items, int count, const s2tc_options* opt, void* stream) {
+  if (!opt || count < 0 || (count > 0 && !items)) {
+    set_error("bad argument");
+    return S2TC_ERR_ARGUMENT;
+  }
+  const s2tc_options o = normalise(*opt);
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+  for (int i = 0; i < count; ++i) {
+    const s2tc_image& im = items[i];
+    const int dxt = format_dxt(im.format);
+    if (dxt < 0) {
+      set_error("bad destination format in item " + std::to_string(i));
+      return S2TC_ERR_FORMAT;
+    }
+    if (im.width <= 0 || im.height <= 0) continue;
+    const int st = s2tc::compress_device_locked(c, im.srccomps, im.width, im.height, static_cast<const uint8_t*>(im.src),
+                                                dxt, static_cast<uint8_t*>(im.dst), im.dst_pitch, o, im.rand, s);
+    if (st != S2TC_OK) return st;
+  }
+  return S2TC_OK;
+}
+
 int s2tc_batch_create(s2tc_batch** out, const s2tc_image* items, int count, const s2tc_options* opt) {
   if (!out || !opt || count < 0 || (count > 0 && !items)) {
     set_error("bad argument");
