@@ -221,9 +221,10 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
     ea.rnd = nullptr;
     if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
   } else {
-    // block rows in chunks so the replayed rand words stay bounded
+    // block rows in chunks so the replayed rand words stay bounded (one
+    // chunk when the caller supplies the words)
     const long long row_words = (long long)bw * per_block;
-    int rows_per_chunk = int(std::max(1ll, kRandChunkWords / std::max(1ll, row_words)));
+    int rows_per_chunk = d_rand ? bh : int(std::max(1ll, kRandChunkWords / std::max(1ll, row_words)));
     if (!d_rand) {
       const size_t chunk_bytes = size_t(std::min<long long>(bh, rows_per_chunk)) * row_words * 4;
       if (!c.rnd.reserve(chunk_bytes, "cudaMalloc(rand)")) return ST_OUT_OF_MEMORY;

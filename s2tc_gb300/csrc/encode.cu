@@ -508,8 +508,19 @@ __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
 constexpr int kRandWarps = 4;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
+// Colour distance rows fit in 16 bits for the AVG family (at most
+// 4*31^2 + 4*63^2 + 31^2 = 20681); they are then packed two per word.
+constexpr bool kSmallDist = kMetric == CD_AVG || kMetric == CD_W0AVG || kMetric == CD_WAVG;
+constexpr int kRowBytes = kSmallDist ? 32 : 64;
+
+// Candidates are deduplicated through a per-warp table indexed by the value
+// inside the block's bounding box when the box has at most kDedupSlots
+// values (first occurrence and first repeat per value).
+constexpr int kDedupSlots = 512;
+constexpr int kDedupWords = 2 * kDedupSlots;
+
 struct RandLayout {
-  size_t p, c, a, d, e, bytes;  // section offsets and bytes per warp
+  size_t p, c, a, d, e, u, t, bytes;  // section offsets and bytes per warp
 };
 
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -520,8 +531,10 @@ __host__ __device__ __forceinline__ RandLayout rand_layout(int m) {
   L.c = align16(L.p + size_t(m) * sizeof(P));          // prepared candidates
   L.a = align16(L.c + size_t(m) * sizeof(uint16_t));   // candidate colours, 5:6:5
   L.d = align16(L.a + size_t(m));                       // candidate alphas
-  L.e = align16(L.d + size_t(m) * 16 * sizeof(int32_t));  // colour distance rows
-  L.bytes = align16(L.e + size_t(m) * 16);              // alpha rows (bytes)
+  L.e = align16(L.d + size_t(m) * kRowBytes);          // colour distance rows
+  L.u = align16(L.e + size_t(m) * 32);                  // alpha rows (16-bit)
+  L.t = align16(L.u + size_t(m) * 2 * sizeof(uint16_t));  // unique colour / alpha indices
+  L.bytes = align16(L.t + kDedupWords * sizeof(uint32_t));  // dedup table
   return L;
 }
 
@@ -676,8 +689,134 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
   return v;
 }
 
+__device__ __forceinline__ uint32_t vmin_u16x2(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+// Sum over the 16 inputs of min(row a, row b).
+__device__ __forceinline__ int32_t pair_sum(const int4* a, const int4* b) {
+  int32_t s = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    s = wadd(s, min(a[q].x, b[q].x));
+    s = wadd(s, min(a[q].y, b[q].y));
+    s = wadd(s, min(a[q].z, b[q].z));
+    s = wadd(s, min(a[q].w, b[q].w));
+  }
+  return s;
+}
+// Same for rows of sixteen 16-bit values (two per word).
+__device__ __forceinline__ uint32_t pair_sum16(const uint4* a, const uint4* b) {
+  uint32_t s = 0;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    s = __dp2a_lo(vmin_u16x2(a[q].x, b[q].x), 0x0101u, s);
+    s = __dp2a_lo(vmin_u16x2(a[q].y, b[q].y), 0x0101u, s);
+    s = __dp2a_lo(vmin_u16x2(a[q].z, b[q].z), 0x0101u, s);
+    s = __dp2a_lo(vmin_u16x2(a[q].w, b[q].w), 0x0101u, s);
+  }
+  return s;
+}
+// Sum over the 16 inputs of min(row a, row b)^2 for alpha rows (values <= 255
+// in 16-bit halves): four minima packed as bytes, squared and summed by dp4a.
+__device__ __forceinline__ uint32_t pair_sq_sum16(const uint4* a, const uint4* b) {
+  uint32_t s = 0;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    uint32_t v = __byte_perm(vmin_u16x2(a[q].x, b[q].x), vmin_u16x2(a[q].y, b[q].y), 0x6420);
+    s = __dp4a(v, v, s);
+    v = __byte_perm(vmin_u16x2(a[q].z, b[q].z), vmin_u16x2(a[q].w, b[q].w), 0x6420);
+    s = __dp4a(v, v, s);
+  }
+  return s;
+}
+
+// Walks every pair i < j < mm: 8-row tiles (I, J), I <= J, four groups of
+// eight lanes per warp, each group one tile at a time; lane r of a group owns
+// row I*8 + r and visits the tile's eight partner rows.  `load(k, row)` reads
+// row k, `sum(a, b)` combines two rows, `visit(i, j, s)` sees every pair once.
+template <class RowT, class Load, class Sum, class Visit>
+__device__ __forceinline__ void tiled_pairs(int mm, int lane, Load load, Sum sum, Visit visit) {
+  const int g = lane >> 3, r = lane & 7;
+  const int nblk = (mm + 7) >> 3;
+  const int T = nblk * (nblk + 1) / 2;
+  for (int t0 = 0; t0 < T; t0 += 4) {
+    const int t = t0 + g;
+    int I = 0, rem = t;
+    while (I < nblk && rem >= nblk - I) {
+      rem -= nblk - I;
+      ++I;
+    }
+    const bool ok = t < T;
+    const int J = I + rem;
+    const int i = I * 8 + r;
+    RowT ri;
+    load(min(i, mm - 1), ri);
+    for (int jj = 0; jj < 8; ++jj) {
+      const int j = J * 8 + jj;
+      RowT rj;
+      load(min(j, mm - 1), rj);
+      const auto v = sum(ri, rj);
+      if (ok && j < mm && j > i) visit(i, j, v);
+    }
+  }
+}
+
+struct RowI32 {
+  int4 q[4];
+};
+struct RowU16 {
+  uint4 q[2];
+};
+
+// Unique candidates in index order.  Equal candidates have equal distance
+// rows under a symmetric metric, hence equal pair sums, and the reference's
+// first minimum is then always a pair of first occurrences (i, j) or a pair
+// (x, y) of a value's first occurrence and its first repeat (its sum is the
+// row sum of x).  `slot(j)` maps candidate j into [0, nslots) (equal slots
+// for equal candidates); without a table (nslots == 0) every candidate is
+// unique.  Writes the unique indices to `uniq`, and for each unique x its
+// first repeat (or 0xFFFFFFFF) to tab[kDedupSlots + slot(x)]; returns the count.
+template <class Slot>
+__device__ __forceinline__ int dedup(int mm, int lane, int nslots, Slot slot, uint16_t* uniq, uint32_t* tab) {
+  if (nslots == 0) {
+    for (int j = lane; j < mm; j += 32) uniq[j] = uint16_t(j);
+    __syncwarp();
+    return mm;
+  }
+  uint32_t* first = tab;
+  uint32_t* rep = tab + kDedupSlots;
+  for (int k = lane; k < nslots; k += 32) {
+    first[k] = 0xFFFFFFFFu;
+    rep[k] = 0xFFFFFFFFu;
+  }
+  __syncwarp();
+  for (int j = lane; j < mm; j += 32) atomicMin(first + slot(j), uint32_t(j));
+  __syncwarp();
+  int nu = 0;
+  for (int base = 0; base < mm; base += 32) {
+    const int j = base + lane;
+    bool u = false;
+    if (j < mm) {
+      const int sj = slot(j);
+      u = first[sj] == uint32_t(j);
+      if (!u) atomicMin(rep + sj, uint32_t(j));
+    }
+    const unsigned bal = __ballot_sync(kFull, u);
+    if (u) uniq[nu + __popc(bal & ((1u << lane) - 1u))] = uint16_t(j);
+    nu += __popc(bal);
+  }
+  __syncwarp();
+  return nu;
+}
+
+#ifndef S2TC_RAND_MINBLOCKS
+#define S2TC_RAND_MINBLOCKS 1
+#endif
 template <int DXT, int REFINE>
-__global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeWork w, int m) {
+__global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode_rand(EncodeWork w, int m) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const RandLayout L = rand_layout(m);
@@ -685,8 +824,11 @@ __global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeWork w, i
   P* sP = reinterpret_cast<P*>(base + L.p);
   uint16_t* sC = reinterpret_cast<uint16_t*>(base + L.c);
   uint8_t* sA = base + L.a;
-  int32_t* sD = reinterpret_cast<int32_t*>(base + L.d);
-  uint8_t* sE = base + L.e;
+  unsigned char* sD = base + L.d;  // colour rows, kRowBytes each (row a: a-th unique candidate)
+  unsigned char* sE = base + L.e;  // alpha rows, 32 bytes each
+  uint16_t* sUc = reinterpret_cast<uint16_t*>(base + L.u);  // unique colour candidates
+  uint16_t* sUa = sUc + m;                                   // unique alpha candidates
+  uint32_t* sTab = reinterpret_cast<uint32_t*>(base + L.t);
   const int nrandom = w.nrandom;
   const int stride = DXT == DXT5 ? 4 : 3;
   const long long nb = w.total;
@@ -751,8 +893,18 @@ __global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeWork w, i
       if (DXT == DXT5) sA[j] = uint8_t(alo + int(__ldg(r + 3) % uint32_t(la)));
     }
     __syncwarp();
+    // deduplicate the colour candidates (symmetric metrics, small boxes)
+    const int cbox = lr * lg * lb;
+    const int ncs = (kSymmetric && cbox <= kDedupSlots) ? cbox : 0;
+    const int nuc = dedup(mm, lane, ncs,
+                          [&](int j) {
+                            const C3 q = unpack565(sC[j]);
+                            return ((q.r - lo.r) * lg + (q.g - lo.g)) * lb + (q.b - lo.b);
+                          },
+                          sUc, sTab);
     // distance rows against the inputs (:375-392); entries k >= n are 0
-    for (int i = lane; i < mm; i += 32) {
+    for (int ua = lane; ua < nuc; ua += 32) {
+      const int i = sUc[ua];
       const P pi = sP[i];
       int32_t row[16];
 #pragma unroll
@@ -764,68 +916,98 @@ __global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeWork w, i
         }
         row[k] = d;
       }
-      int4* dr = reinterpret_cast<int4*>(sD + size_t(i) * 16);
+      if (kSmallDist) {
+        uint4* dr = reinterpret_cast<uint4*>(sD + size_t(ua) * kRowBytes);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dr[q] = make_int4(row[4 * q], row[4 * q + 1], row[4 * q + 2], row[4 * q + 3]);
-      if (DXT == DXT5) {
-        const int ai = sA[i];
-        uint32_t w[4] = {0, 0, 0, 0};
+        for (int q = 0; q < 2; ++q)
+          dr[q] = make_uint4(uint32_t(row[8 * q]) | (uint32_t(row[8 * q + 1]) << 16),
+                             uint32_t(row[8 * q + 2]) | (uint32_t(row[8 * q + 3]) << 16),
+                             uint32_t(row[8 * q + 4]) | (uint32_t(row[8 * q + 5]) << 16),
+                             uint32_t(row[8 * q + 6]) | (uint32_t(row[8 * q + 7]) << 16));
+      } else {
+        int4* dr = reinterpret_cast<int4*>(sD + size_t(ua) * kRowBytes);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          if (k < n) {
-            const int ak = sA[k];
-            const uint32_t v = uint32_t(min(abs(ai - ak), min(ak, 255 - ak)));
-            w[k >> 2] |= v << (8 * (k & 3));
-          }
-        }
-        *reinterpret_cast<uint4*>(sE + size_t(i) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+        for (int q = 0; q < 4; ++q) dr[q] = make_int4(row[4 * q], row[4 * q + 1], row[4 * q + 2], row[4 * q + 3]);
       }
     }
     __syncwarp();
 
-    // colour pair search
+    // colour pair search: the smallest (sum, i, j) is the pair the
+    // reference keeps when no sum is negative
     int ci, cj;
     {
       uint64_t best = ~0ull;
       bool neg = false;
-      for (int r0 = 0; r0 < mm; r0 += 32) {
-        const int i = r0 + lane;
-        int32_t ri[16];
-        if (i < mm) {
-          const int4* q = reinterpret_cast<const int4*>(sD + size_t(i) * 16);
+      if (kSmallDist) {
+        tiled_pairs<RowU16>(
+            nuc, lane,
+            [&](int k, RowU16& rw) {
+              const uint4* q = reinterpret_cast<const uint4*>(sD + size_t(k) * kRowBytes);
+              rw.q[0] = q[0];
+              rw.q[1] = q[1];
+            },
+            [](const RowU16& x, const RowU16& y) { return pair_sum16(x.q, y.q); },
+            [&](int a, int b, uint32_t v) {
+              const uint64_t key = (uint64_t(v) << 32) | (uint32_t(sUc[a]) << 16) | uint32_t(sUc[b]);
+              best = key < best ? key : best;
+            });
+      } else {
+        tiled_pairs<RowI32>(
+            nuc, lane,
+            [&](int k, RowI32& rw) {
+              const int4* q = reinterpret_cast<const int4*>(sD + size_t(k) * kRowBytes);
 #pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const int4 v = q[t];
-            ri[4 * t] = v.x; ri[4 * t + 1] = v.y; ri[4 * t + 2] = v.z; ri[4 * t + 3] = v.w;
-          }
-        }
-        for (int j = r0 + 1; j < mm; ++j) {
-          const int4* q = reinterpret_cast<const int4*>(sD + size_t(j) * 16);
-          int32_t sum = 0;
+              for (int t = 0; t < 4; ++t) rw.q[t] = q[t];
+            },
+            [](const RowI32& x, const RowI32& y) { return pair_sum(x.q, y.q); },
+            [&](int a, int b, int32_t v) {
+              neg |= v < 0;
+              const uint64_t key = (uint64_t(uint32_t(v)) << 32) | (uint32_t(sUc[a]) << 16) | uint32_t(sUc[b]);
+              if (v >= 0 && key < best) best = key;
+            });
+      }
+      if (ncs > 0) {
+        // pairs of a value's first occurrence and its first repeat: the row sum
+        for (int ua = lane; ua < nuc; ua += 32) {
+          const int x = sUc[ua];
+          const C3 q = unpack565(sC[x]);
+          const uint32_t y = sTab[kDedupSlots + ((q.r - lo.r) * lg + (q.g - lo.g)) * lb + (q.b - lo.b)];
+          if (y == 0xFFFFFFFFu) continue;
+          int32_t v = 0;
+          if (kSmallDist) {
+            const uint4* r = reinterpret_cast<const uint4*>(sD + size_t(ua) * kRowBytes);
+            uint32_t t = 0;
 #pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const int4 v = q[t];
-            sum = wadd(sum, min(ri[4 * t], v.x));
-            sum = wadd(sum, min(ri[4 * t + 1], v.y));
-            sum = wadd(sum, min(ri[4 * t + 2], v.z));
-            sum = wadd(sum, min(ri[4 * t + 3], v.w));
+            for (int h = 0; h < 2; ++h) {
+              t = __dp2a_lo(r[h].x, 0x0101u, t);
+              t = __dp2a_lo(r[h].y, 0x0101u, t);
+              t = __dp2a_lo(r[h].z, 0x0101u, t);
+              t = __dp2a_lo(r[h].w, 0x0101u, t);
+            }
+            v = int32_t(t);
+          } else {
+            const int32_t* r = reinterpret_cast<const int32_t*>(sD + size_t(ua) * kRowBytes);
+            for (int k = 0; k < 16; ++k) v = wadd(v, r[k]);
           }
-          if (i < mm && j > i) {
-            neg |= sum < 0;
-            const uint64_t key = (uint64_t(uint32_t(sum)) << 32) | (uint32_t(i) << 16) | uint32_t(j);
-            if (sum >= 0 && key < best) best = key;
-          }
+          neg |= v < 0;
+          const uint64_t key = (uint64_t(uint32_t(v)) << 32) | (uint32_t(x) << 16) | y;
+          if (v >= 0 && key < best) best = key;
         }
       }
-      if (__any_sync(kFull, neg)) {
+      if (!kSmallDist && __any_sync(kFull, neg)) {
         // negative sums: replay the reference's rule in pair order on one lane
         int bi = 0, bj = 1;
         if (lane == 0) {
+          // rows of the original candidates, recomputed (rare path)
+          auto dist_ik = [&](int i, int k) -> int32_t {
+            if (k >= n || k == i) return 0;
+            return (kSymmetric || i >= n || i < k) ? pdist<kMetric>(sP[i], sP[k]) : pdist<kMetric>(sP[k], sP[i]);
+          };
           int32_t bestsum = -1;
           for (int i = 0; i < mm; ++i)
             for (int j = i + 1; j < mm; ++j) {
               int32_t sum = 0;
-              for (int k = 0; k < 16; ++k) sum = wadd(sum, min(sD[i * 16 + k], sD[j * 16 + k]));
+              for (int k = 0; k < 16; ++k) sum = wadd(sum, min(dist_ik(i, k), dist_ik(j, k)));
               if (bestsum < 0 || sum < bestsum) {
                 bestsum = sum;
                 bi = i;
@@ -844,24 +1026,51 @@ __global__ void __launch_bounds__(32 * kRandWarps) k_encode_rand(EncodeWork w, i
     C3 c0 = unpack565(sC[ci]), c1 = unpack565(sC[cj]);
     int a0 = 0, a1 = 0;
     if (DXT == DXT5) {
-      // alpha pair search (:415-478); sums of squares of bytes never overflow
-      uint64_t best = ~0ull;
-      for (int r0 = 0; r0 < mm; r0 += 32) {
-        const int i = r0 + lane;
-        uint4 ri = make_uint4(0, 0, 0, 0);
-        if (i < mm) ri = *reinterpret_cast<const uint4*>(sE + size_t(i) * 16);
-        for (int j = r0 + 1; j < mm; ++j) {
-          const uint4 rj = *reinterpret_cast<const uint4*>(sE + size_t(j) * 16);
-          uint32_t v, sum = 0;
-          v = __vminu4(ri.x, rj.x); sum = __dp4a(v, v, sum);
-          v = __vminu4(ri.y, rj.y); sum = __dp4a(v, v, sum);
-          v = __vminu4(ri.z, rj.z); sum = __dp4a(v, v, sum);
-          v = __vminu4(ri.w, rj.w); sum = __dp4a(v, v, sum);
-          if (i < mm && j > i) {
-            const uint64_t key = (uint64_t(sum) << 32) | (uint32_t(i) << 16) | uint32_t(j);
-            if (key < best) best = key;
-          }
+      // alpha pair search (:415-478) over the distinct alpha values; sums of
+      // squares of bytes never overflow
+      __syncwarp();
+      const int nua = dedup(mm, lane, 256, [&](int j) { return int(sA[j]); }, sUa, sTab);
+      for (int ua = lane; ua < nua; ua += 32) {
+        const int ai = sA[sUa[ua]];
+        uint32_t v[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const int ak = sA[k];
+          v[k] = k < n ? uint32_t(min(abs(ai - ak), min(ak, 255 - ak))) : 0u;
         }
+        uint4* er = reinterpret_cast<uint4*>(sE + size_t(ua) * 32);
+        er[0] = make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16), v[6] | (v[7] << 16));
+        er[1] = make_uint4(v[8] | (v[9] << 16), v[10] | (v[11] << 16), v[12] | (v[13] << 16), v[14] | (v[15] << 16));
+      }
+      __syncwarp();
+      uint64_t best = ~0ull;
+      tiled_pairs<RowU16>(
+          nua, lane,
+          [&](int k, RowU16& rw) {
+            const uint4* q = reinterpret_cast<const uint4*>(sE + size_t(k) * 32);
+            rw.q[0] = q[0];
+            rw.q[1] = q[1];
+          },
+          [](const RowU16& x, const RowU16& y) { return pair_sq_sum16(x.q, y.q); },
+          [&](int a, int b, uint32_t v) {
+            const uint64_t key = (uint64_t(v) << 32) | (uint32_t(sUa[a]) << 16) | uint32_t(sUa[b]);
+            best = key < best ? key : best;
+          });
+      for (int ua = lane; ua < nua; ua += 32) {
+        const int x = sUa[ua];
+        const uint32_t y = sTab[kDedupSlots + sA[x]];
+        if (y == 0xFFFFFFFFu) continue;
+        const uint4* r = reinterpret_cast<const uint4*>(sE + size_t(ua) * 32);
+        uint32_t t = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t p = __byte_perm(r[h].x, r[h].y, 0x6420);
+          t = __dp4a(p, p, t);
+          p = __byte_perm(r[h].z, r[h].w, 0x6420);
+          t = __dp4a(p, p, t);
+        }
+        const uint64_t key = (uint64_t(t) << 32) | (uint32_t(x) << 16) | y;
+        best = key < best ? key : best;
       }
       best = warp_min_u64(best);
       a0 = sA[(best >> 16) & 0xFFFF];
@@ -902,6 +1111,21 @@ size_t rand_smem_bytes(int m) {
   return bytes <= 200 * 1024 ? bytes : 0;
 }
 
+// Raises the kernel's dynamic shared memory limit only when a launch needs more
+// than any earlier one (the attribute persists), then launches.
+template <int DXT, int REFINE>
+cudaError_t launch_rand(const EncodeWork& a, int m, size_t smem, unsigned grid, cudaStream_t s) {
+  static int limit = 48 * 1024;
+  if (int(smem) > limit) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_encode_rand<DXT, REFINE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    limit = int(smem);
+  }
+  k_encode_rand<DXT, REFINE><<<grid, 32 * kRandWarps, smem, s>>>(a, m);
+  return cudaGetLastError();
+}
+
 template <int DXT, bool NORMAL>
 cudaError_t launch_r(const EncodeWork& a, int refine, cudaStream_t s) {
   const long long nb = a.total;
@@ -914,24 +1138,11 @@ cudaError_t launch_r(const EncodeWork& a, int refine, cudaStream_t s) {
     if (smem > 0) {
       count_launches(1);
       const unsigned rgrid = unsigned(std::min<long long>((nb + kRandWarps - 1) / kRandWarps, 152ll * 64));
-      cudaError_t e = cudaSuccess;
       switch (refine) {
-        case RF_NEVER:
-          e = cudaFuncSetAttribute(k_encode_rand<DXT, RF_NEVER>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-          if (e == cudaSuccess) k_encode_rand<DXT, RF_NEVER><<<rgrid, 32 * kRandWarps, smem, s>>>(a, m);
-          break;
-        case RF_LOOP:
-          e = cudaFuncSetAttribute(k_encode_rand<DXT, RF_LOOP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-          if (e == cudaSuccess) k_encode_rand<DXT, RF_LOOP><<<rgrid, 32 * kRandWarps, smem, s>>>(a, m);
-          break;
-        default:
-          e = cudaFuncSetAttribute(k_encode_rand<DXT, RF_ALWAYS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(smem));
-          if (e == cudaSuccess) k_encode_rand<DXT, RF_ALWAYS><<<rgrid, 32 * kRandWarps, smem, s>>>(a, m);
-          break;
+        case RF_NEVER: return launch_rand<DXT, RF_NEVER>(a, m, smem, rgrid, s);
+        case RF_LOOP: return launch_rand<DXT, RF_LOOP>(a, m, smem, rgrid, s);
+        default: return launch_rand<DXT, RF_ALWAYS>(a, m, smem, rgrid, s);
       }
-      if (e != cudaSuccess) return e;
-      return cudaGetLastError();
     }
   }
   if (NORMAL && a.nrandom <= 0) {

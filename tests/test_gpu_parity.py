@@ -293,3 +293,18 @@ def test_batch_repeated_runs(lib):
             assert np.array_equal(im["dst"].cpu().numpy(), want)
     assert b.kernels >= 2
     b.close()
+
+
+@pytest.mark.parametrize("metric", range(8))
+def test_random_candidates_repeated_values(lib, oracle, metric):
+    """Blocks with few distinct colours and alphas: the random candidates
+    repeat, and the warp kernel searches the distinct ones only."""
+    rng = np.random.default_rng(100 + metric)
+    for fmt in (0x83F1, 0x83F2, 0x83F3):
+        for kind in (2, 3, 1):
+            w, h = int(rng.integers(4, 21)), int(rng.integers(4, 21))
+            img = cases.image(rng, w, h, 4, kind)
+            for nr, refine in ((64, 1), (9, 2)):
+                a = gpu_compress(4, w, h, img, fmt, 0, metric, nr, refine, 5)
+                b = oracle.compress(4, w, h, img, fmt, 0, metric, nr, refine, seed=5)
+                assert np.array_equal(a, b), (hex(fmt), kind, nr)
