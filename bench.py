@@ -59,6 +59,12 @@ WORKLOADS = {
     # mixed DXT1/DXT3/DXT5, RGB8/RGBA8: one batched graph launch per step
     "mip_chains_256_wavg_rand64_always": dict(
         w=0, h=0, sc=0, fmt=0, dither=1, metric=5, nrandom=64, refine=1, gen="mips", seed=3, count=256),
+    # requests of log-uniform size 64..4096, DXT1/DXT5, WAVG/SRGB_MIXED/NORMALMAP,
+    # through the continuous-batching request loop under a 32 GB budget; a
+    # step is 1000 requests
+    "serving_requests_64_4096_budget32g": dict(
+        w=0, h=0, sc=4, fmt=0, dither=1, metric=-1, nrandom=-1, refine=1, gen="serving", seed=5,
+        budget=32 << 30, per_step=1000),
 }
 DEFAULT_WORKLOAD = "value_noise_4096_dxt5_srgb_mixed_all16_loop"
 FMT_NAMES = {0x83F0: "DXT1(RGB)", 0x83F1: "DXT1", 0x83F2: "DXT3", 0x83F3: "DXT5"}
@@ -86,6 +92,13 @@ def algorithmic_bytes_per_texel(wl: dict) -> float:
 
 def config_dict(wl_name: str, wl: dict) -> dict:
     import s2tc_gb300 as s2
+    if wl["gen"] == "serving":
+        return {"workload": wl_name, "requests_per_step": wl["per_step"], "sizes": "log-uniform 64..4096 per side",
+                "formats": "DXT1/DXT5 uniform", "colordist": "WAVG/SRGB_MIXED/NORMALMAP uniform",
+                "dither": "SIMPLE", "random_colors": -1, "refine": "ALWAYS", "budget_bytes": wl["budget"],
+                "pixels": "per-request windows of one pre-generated 4096x8192 plain (noise + gradient) image at "
+                          "seeded offsets",
+                "l2": "the requests' inputs (GBs per step) exceed the 129 MB L2"}
     if wl["gen"] == "mips":
         return {"workload": wl_name, "textures": wl["count"], "base_sizes": "log-uniform 4..2048, aspect <= 4:1",
                 "levels": "full mip chains to 1x1", "formats": "DXT1/DXT3/DXT5 by thirds",
@@ -382,6 +395,182 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------- serving workload
+
+def _lindley(arrivals, service):
+    """Latencies of a single FIFO server that takes the requests one at a
+    time (the per-request path) under the given arrival times."""
+    lat, free = [], 0.0
+    for a, s in zip(arrivals, service):
+        start = max(a, free)
+        free = start + s
+        lat.append(free - a)
+    return lat
+
+
+def run_serving_workload(args, wl_name: str, wl: dict) -> None:
+    """The continuous-batching request loop (s2tc_server_*) against the plain
+    per-request path (one tx_compress_dxtn per request): saturated
+    throughput, then Poisson arrivals at fractions of that rate with the
+    server's own p50/p99 latencies (submit to blocks in host memory)."""
+    import threading
+    import zlib
+    import torch
+    import s2tc_gb300 as s2
+    from s2tc_gb300 import workloads
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    nreq = args.steps * wl["per_step"]
+    reqs = workloads.serving_requests(wl["seed"], count=nreq, lo=64, hi=4096)
+    # one pinned pool of pixels; request i reads a window at a seeded offset
+    pool_img = np.concatenate([workloads.plain_rgba(wl["seed"], 4096, 4096),
+                               workloads.plain_rgba(wl["seed"] + 1, 4096, 4096)]).reshape(-1)
+    pool = torch.from_numpy(pool_img).pin_memory()
+    half = pool_img.nbytes // 2
+    rng = np.random.default_rng(wl["seed"])
+    offs = (rng.integers(0, half // 256, nreq) * 256).tolist()
+    sizes = [(r["width"], r["height"], r["fmt"]) for r in reqs]
+    opts = {m: s2.options(wl["dither"], m, wl["nrandom"], wl["refine"]) for m in (3, 5, 7)}
+    out_sizes = [s2.compressed_size(w, h, f) for w, h, f in sizes]
+    texels = [w * h for w, h, _ in sizes]
+    base = pool.data_ptr()
+    ring_bytes = 2 << 30
+    ring = torch.empty(ring_bytes, dtype=torch.uint8).pin_memory()
+    rbase = ring.data_ptr()
+    lib = s2.load()
+
+    def serve(arrivals, check=None):
+        """Submit every request at its arrival time (None: all at once);
+        outputs go to a ring of pinned memory that the waiter frees in order."""
+        srv = s2.Server(wl["budget"])
+        ids = [0] * nreq
+        lat = [0.0] * nreq
+        cond = threading.Condition()
+        state = {"consumed": 0, "submitted": 0}
+        dst_off = [0] * nreq
+        crcs = {}
+
+        def waiter():
+            for i in range(nreq):
+                with cond:
+                    cond.wait_for(lambda: state["submitted"] > i)
+                lat[i] = srv.wait(ids[i])
+                if check is not None and i in check:
+                    crcs[i] = zlib.crc32(ctypes.string_at(rbase + dst_off[i], out_sizes[i]))
+                with cond:
+                    state["consumed"] = i + 1
+                    cond.notify_all()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        head = 0
+
+        def fits(i, n):
+            # unconsumed outputs occupy the arc from the oldest one's offset
+            # (tail) up to head
+            c = state["consumed"]
+            if c >= i:
+                return True
+            tail = dst_off[c]
+            if tail < head:
+                return head + n <= ring_bytes
+            return tail > head and head + n <= tail
+
+        t0 = time.perf_counter()
+        for i in range(nreq):
+            n = out_sizes[i]
+            if head + n > ring_bytes:
+                head = 0
+            if not fits(i, n):
+                with cond:
+                    cond.wait_for(lambda: fits(i, n))
+            if arrivals is not None:
+                due = t0 + arrivals[i]
+                while True:
+                    dt = due - time.perf_counter()
+                    if dt <= 0:
+                        break
+                    time.sleep(dt if dt > 2e-4 else 0)
+            w, h, f = sizes[i]
+            dst_off[i] = head
+            ids[i] = srv.submit(base + offs[i], 4, w, h, f, opts[reqs[i]["metric"]], rbase + head)
+            head += (n + 255) // 256 * 256
+            with cond:
+                state["submitted"] = i + 1
+                cond.notify_all()
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        return wall, lat, st, crcs
+
+    # the per-request path: one synchronous tx_compress_dxtn per request
+    check = set(range(0, nreq, 10))
+    want = {}
+    service = [0.0] * nreq
+    out1 = torch.empty(max(out_sizes), dtype=torch.uint8).pin_memory()
+    cur = [None]
+
+    def per_request(i):
+        w, h, f = sizes[i]
+        m = reqs[i]["metric"]
+        if cur[0] != m:
+            s2.set_env(wl["dither"], m, wl["nrandom"], wl["refine"])
+            cur[0] = m
+        lib.tx_compress_dxtn(4, w, h, base + offs[i], f, out1.data_ptr(), 0)
+
+    for i in range(min(nreq, 50)):
+        per_request(i)
+    for i in range(nreq):
+        t0 = time.perf_counter()
+        per_request(i)
+        service[i] = time.perf_counter() - t0
+        if i in check:
+            want[i] = zlib.crc32(ctypes.string_at(out1.data_ptr(), out_sizes[i]))
+    t_single = sum(service)
+    total_tex = sum(texels)
+
+    serve(None)  # warm-up: streams, pinned tables, first-use of the kernels
+    l0 = s2.kernel_launches()
+    with ClockSampler(0) as clk:
+        wall, lat, st, crcs = serve(None, check)
+    launches = s2.kernel_launches() - l0
+    bit_exact = all(crcs.get(i) == want[i] for i in check)
+    value = total_tex / wall
+    rate_max = nreq / wall
+    poisson = []
+    for frac in (0.5, 0.8):
+        rate = frac * rate_max
+        arr = np.cumsum(np.random.default_rng(17).exponential(1.0 / rate, nreq)).tolist()
+        pw, plat, pst, _ = serve(arr)
+        single_lat = _lindley(arr, service)
+        poisson.append({"rate_rps": rate, "offered_frac_of_saturation": frac,
+                        "texels_per_s": total_tex / pw,
+                        "p50_ms": float(np.percentile(plat, 50)), "p99_ms": float(np.percentile(plat, 99)),
+                        "rounds": pst["rounds"], "max_inflight_rounds": pst["max_inflight_rounds"],
+                        "per_request_path_p50_ms": 1000 * float(np.percentile(single_lat, 50)),
+                        "per_request_path_p99_ms": 1000 * float(np.percentile(single_lat, 99))})
+    in_b = sum(t * 4 for t in texels)
+    out_b = sum(out_sizes)
+    line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": dict(config_dict(wl_name, wl), requests=nreq, texels=total_tex),
+            "e2e": {"value": value, "unit": "texels/s", "h2d_bytes_per_step": in_b // args.steps,
+                    "d2h_bytes_per_step": out_b // args.steps,
+                    "note": "host buffers in and out; the loop is end to end by construction"},
+            "saturated": {"rounds": st["rounds"], "max_round_requests": st["max_round_requests"],
+                          "max_inflight_rounds": st["max_inflight_rounds"],
+                          "pool_high_water": st["pool_high_water"],
+                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
+            "per_request": {"value": total_tex / t_single, "unit": "texels/s",
+                            "ms_per_request_mean": 1000 * t_single / nreq},
+            "server_over_per_request": value / (total_tex / t_single),
+            "poisson": poisson, "bit_exact_sampled": bit_exact, "bit_exact_requests_checked": len(check),
+            "gpu_launches": launches, "cpu_baseline": None, "clocks": clk.summary(),
+            "roofline": None}
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------- GPU arm
 
 def main() -> None:
@@ -398,13 +587,16 @@ def main() -> None:
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
-        if wl["gen"] == "mips":
+        if wl["gen"] in ("mips", "serving"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times single-image workloads"}))
             return
         run_reference_arm(args, args.workload, wl)
         return
     if wl["gen"] == "mips":
         run_batch_workload(args, args.workload, wl)
+        return
+    if wl["gen"] == "serving":
+        run_serving_workload(args, args.workload, wl)
         return
 
     import torch

@@ -139,6 +139,34 @@ int s2tc_batch_run(s2tc_batch *batch, void *stream);
 int s2tc_batch_kernels(const s2tc_batch *batch);
 void s2tc_batch_destroy(s2tc_batch *batch);
 
+/* ---- serving: a request loop with continuous batching ---- */
+
+typedef struct s2tc_server s2tc_server;
+
+/* Start a server whose requests share `budget_bytes` of device memory (input,
+ * texel words, output and rand words of every admitted request).  A
+ * scheduler thread admits waiting requests in arrival order as memory frees
+ * up and launches each group of admitted requests as one round of batched
+ * kernels; rounds overlap on the GPU.  Pass pinned host buffers so that the
+ * uploads and downloads overlap too. */
+int s2tc_server_create(s2tc_server **out, long long budget_bytes);
+/* Queue one compression (host pixels in, host blocks out, block rows
+ * dst_pitch bytes apart or packed when 0); returns immediately with an id.
+ * Random candidates draw libc rand() here, in submission order.  A request
+ * larger than the whole budget is rejected with S2TC_ERR_TOO_LARGE. */
+int s2tc_server_submit(s2tc_server *server, const void *src, int srccomps, int width, int height,
+		       unsigned int format, const s2tc_options *opt, void *dst, long long dst_pitch,
+		       long long *id);
+/* Block until request `id` is done; its latency (submission to completion)
+ * in milliseconds.  Each id can be waited for once. */
+int s2tc_server_wait(s2tc_server *server, long long id, double *latency_ms);
+/* Rounds launched, requests done, most rounds in flight at once, most
+ * requests in one round, device pool high-water mark in bytes. */
+int s2tc_server_stats(s2tc_server *server, long long *rounds, long long *done, int *max_inflight_rounds,
+		      int *max_round_requests, long long *pool_high_water);
+/* Finish the queued requests and stop. */
+void s2tc_server_destroy(s2tc_server *server);
+
 /* Wait for `stream` (NULL: the library's stream) and report whether any
  * kernel since the last check gave up a bounded wait (S2TC_ERR_TIMEOUT). */
 int s2tc_gpu_synchronize(void *stream);

@@ -125,6 +125,18 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_batch_kernels.restype = c_int
     lib.s2tc_batch_destroy.argtypes = [vp]
     lib.s2tc_batch_destroy.restype = None
+    lib.s2tc_server_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_ll]
+    lib.s2tc_server_create.restype = c_int
+    lib.s2tc_server_submit.argtypes = [vp, vp, c_int, c_int, c_int, c_uint, ctypes.POINTER(Options), vp, c_ll,
+                                       ctypes.POINTER(c_ll)]
+    lib.s2tc_server_submit.restype = c_int
+    lib.s2tc_server_wait.argtypes = [vp, c_ll, ctypes.POINTER(ctypes.c_double)]
+    lib.s2tc_server_wait.restype = c_int
+    lib.s2tc_server_stats.argtypes = [vp, ctypes.POINTER(c_ll), ctypes.POINTER(c_ll), ctypes.POINTER(c_int),
+                                      ctypes.POINTER(c_int), ctypes.POINTER(c_ll)]
+    lib.s2tc_server_stats.restype = c_int
+    lib.s2tc_server_destroy.argtypes = [vp]
+    lib.s2tc_server_destroy.restype = None
     lib.s2tc_last_error.argtypes = []
     lib.s2tc_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -139,7 +151,8 @@ EXPORTED_SYMBOLS = (
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
     "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
     "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
-    "s2tc_batch_kernels", "s2tc_batch_destroy",
+    "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit",
+    "s2tc_server_wait", "s2tc_server_stats", "s2tc_server_destroy",
     "s2tc_last_error",
 )
 
@@ -339,6 +352,58 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "handle", None):
             load().s2tc_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """``s2tc_server_*``: a continuous-batching request loop under a device
+    memory budget.  ``submit`` takes host buffers (numpy arrays or torch CPU
+    tensors; pinned ones let copies overlap) and returns an id; ``wait``
+    returns the latency in milliseconds."""
+
+    def __init__(self, budget_bytes: int):
+        h = ctypes.c_void_p()
+        st = load().s2tc_server_create(ctypes.byref(h), int(budget_bytes))
+        if st != S2TC_OK:
+            raise S2tcError(f"s2tc_server_create failed ({st}): {last_error()}")
+        self.handle = h
+        self._keep = {}
+
+    def submit(self, src, srccomps: int, width: int, height: int, fmt: int, opt: Options, dst,
+               dst_pitch: int = 0) -> int:
+        rid = ctypes.c_longlong()
+        st = load().s2tc_server_submit(self.handle, _addr(src), srccomps, width, height, fmt, ctypes.byref(opt),
+                                       _addr(dst), dst_pitch, ctypes.byref(rid))
+        if st != S2TC_OK:
+            raise S2tcError(f"s2tc_server_submit failed ({st})")
+        self._keep[rid.value] = (src, dst)
+        return rid.value
+
+    def wait(self, rid: int) -> float:
+        lat = ctypes.c_double()
+        st = load().s2tc_server_wait(self.handle, rid, ctypes.byref(lat))
+        self._keep.pop(rid, None)
+        if st != S2TC_OK:
+            raise S2tcError(f"request {rid} failed ({st})")
+        return lat.value
+
+    def stats(self) -> dict:
+        r, d, hw = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        mi, mr = ctypes.c_int(), ctypes.c_int()
+        load().s2tc_server_stats(self.handle, ctypes.byref(r), ctypes.byref(d), ctypes.byref(mi), ctypes.byref(mr),
+                                 ctypes.byref(hw))
+        return {"rounds": r.value, "done": d.value, "max_inflight_rounds": mi.value,
+                "max_round_requests": mr.value, "pool_high_water": hw.value}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            load().s2tc_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -43,6 +43,7 @@ def _units():
     for name in ("dither.cu", "dither_fs.cu", "noalloc.cu"):
         units.append((CSRC / name, OBJ_DIR / (Path(name).stem + ".o"), []))
     units.append((CSRC / "capi.cpp", OBJ_DIR / "capi.o", ["-x", "cu"]))
+    units.append((CSRC / "server.cpp", OBJ_DIR / "server.o", ["-x", "cu"]))
     return units
 
 

@@ -813,7 +813,7 @@ __device__ __forceinline__ int dedup(int mm, int lane, int nslots, Slot slot, ui
 }
 
 #ifndef S2TC_RAND_MINBLOCKS
-#define S2TC_RAND_MINBLOCKS 1
+#define S2TC_RAND_MINBLOCKS 5
 #endif
 template <int DXT, int REFINE>
 __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode_rand(EncodeWork w, int m) {
@@ -948,7 +948,9 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
             },
             [](const RowU16& x, const RowU16& y) { return pair_sum16(x.q, y.q); },
             [&](int a, int b, uint32_t v) {
-              const uint64_t key = (uint64_t(v) << 32) | (uint32_t(sUc[a]) << 16) | uint32_t(sUc[b]);
+              if (v > uint32_t(best >> 32)) return;  // cannot win; skip the index lookups
+              const uint32_t ia = ncs ? sUc[a] : a, ib = ncs ? sUc[b] : b;
+              const uint64_t key = (uint64_t(v) << 32) | (ia << 16) | ib;
               best = key < best ? key : best;
             });
       } else {
@@ -962,8 +964,10 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
             [](const RowI32& x, const RowI32& y) { return pair_sum(x.q, y.q); },
             [&](int a, int b, int32_t v) {
               neg |= v < 0;
-              const uint64_t key = (uint64_t(uint32_t(v)) << 32) | (uint32_t(sUc[a]) << 16) | uint32_t(sUc[b]);
-              if (v >= 0 && key < best) best = key;
+              if (v < 0 || uint32_t(v) > uint32_t(best >> 32)) return;
+              const uint32_t ia = ncs ? sUc[a] : a, ib = ncs ? sUc[b] : b;
+              const uint64_t key = (uint64_t(uint32_t(v)) << 32) | (ia << 16) | ib;
+              best = key < best ? key : best;
             });
       }
       if (ncs > 0) {
@@ -1053,6 +1057,7 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
           },
           [](const RowU16& x, const RowU16& y) { return pair_sq_sum16(x.q, y.q); },
           [&](int a, int b, uint32_t v) {
+            if (v > uint32_t(best >> 32)) return;
             const uint64_t key = (uint64_t(v) << 32) | (uint32_t(sUa[a]) << 16) | uint32_t(sUa[b]);
             best = key < best ? key : best;
           });
