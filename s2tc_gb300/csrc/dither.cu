@@ -3,18 +3,22 @@
 //
 // DITHER_NONE is elementwise.  DITHER_SIMPLE is one serial error-diffusion
 // chain per channel over the whole image in raster order; it is computed here
-// as an exact single-pass scan:
-//   - a channel's carried error takes few values (red/blue: -7..7, green:
-//     -3..3, 4-bit alpha: -15..15), so the effect of a run of texels on it is a
-//     small table state -> state; tables compose;
-//   - each thread builds the table of its 64-texel segment, the CTA composes
-//     them (Hillis-Steele in shared memory), tiles chain their aggregates with
-//     a decoupled look-back, and every thread then replays its segment from
-//     its exact start state;
-//   - the 5- and 6-bit channels run all start states at once, four per 32-bit
-//     word (one byte each): one texel step is then a handful of byte-parallel
-//     adds and masks driven by constants that depend only on the source byte
-//     (see swar_step);
+// as an exact single-pass scan over tiles of kTile texels, one CTA per tile:
+//   - the tile is read from HBM once, with coalesced vector loads, into shared
+//     memory as one RGBA word per texel;
+//   - thread t owns the kSeg consecutive texels starting at kSeg * t.  kSeg is
+//     odd, so at every step the 32 lanes of a warp read 32 distinct banks;
+//   - a channel's carried error takes few values (red/blue -7..7, green -3..3,
+//     4-bit alpha -15..15), so the effect of a run of texels on it is a small
+//     table "start state -> end state".  Each thread computes its segment's
+//     table for all start states at once, four states per 32-bit word (one
+//     byte each, see swar_step / swar_step4);
+//   - tables compose with byte gathers (prmt): warps scan their lanes' tables
+//     with shuffles, warp 0 scans the warps' aggregates, and tiles chain their
+//     aggregates through a decoupled look-back in global memory;
+//   - every thread then replays its segment from its exact start state and
+//     overwrites its texels in shared memory with the 5:6:5 words, which the
+//     CTA writes out with coalesced vector stores;
 //   - the 1-bit alpha chain (diffuse1) is a rotation: its carried error after
 //     k texels is ((sum of sources + 127) mod 255) - 127, so its "table" is a
 //     sum mod 255.
@@ -32,14 +36,13 @@ namespace s2tc {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSeg = 64;  // texels per thread, contiguous in raster order
-constexpr int kTile = kThreads * kSeg;
+constexpr int kWarps = kThreads / 32;
+constexpr int kSeg = 65;                // texels per thread (odd: conflict-free)
+constexpr int kTile = kThreads * kSeg;  // 16640 texels per tile
+constexpr int kRecWords = 18;           // red 4, green 2, blue 4, alpha 8 words
+constexpr int kRec = 4 * kRecWords;     // bytes per aggregate record in global memory
 
-// Table layout (bytes) inside one 72-byte record: red 15 states at 0, green 7
-// at 16, blue 15 at 24, alpha at 40 (31 states for 4-bit, or one byte holding
-// the mod-255 sum for 1-bit).
-constexpr int kOffR = 0, kOffG = 16, kOffB = 24, kOffA = 40;
-constexpr int kRec = 72;
+// ------------------------------------------------------------ scalar steps
 
 // One step of the 1-D error diffusion (s2tc_algorithm.cpp:1198-1207).
 template <int SHIFT>
@@ -51,76 +54,7 @@ __device__ __forceinline__ int qstep(int& d, int src) {
   return q;
 }
 
-template <int SHIFT>
-struct QChan {
-  static constexpr int kOff = (1 << SHIFT) - 1;  // largest carried error
-  static constexpr int kStates = 2 * kOff + 1;
-};
-
-__device__ __forceinline__ int chan_of(uint32_t px, int c) { return int((px >> (8 * c)) & 0xFF); }
-
-// Table of one channel over the thread's segment: entry s is the end state
-// when the segment starts in state s.
-template <int SHIFT>
-__device__ __forceinline__ void seg_table(const uint32_t* px, int nvalid, int c, uint8_t* out) {
-  using Q = QChan<SHIFT>;
-#pragma unroll 1
-  for (int s = 0; s < Q::kStates; ++s) {
-    int d = s - Q::kOff;
-#pragma unroll
-    for (int k = 0; k < kSeg; ++k)
-      if (k < nvalid) qstep<SHIFT>(d, chan_of(px[k], c));
-    out[s] = uint8_t(d + Q::kOff);
-  }
-}
-
-// dst = apply `first`, then `second`.
-template <int AK>
-__device__ __forceinline__ void compose(const uint8_t* first, const uint8_t* second, uint8_t* dst) {
-#pragma unroll 1
-  for (int s = 0; s < QChan<3>::kStates; ++s) {
-    dst[kOffR + s] = second[kOffR + first[kOffR + s]];
-    dst[kOffB + s] = second[kOffB + first[kOffB + s]];
-  }
-#pragma unroll 1
-  for (int s = 0; s < QChan<2>::kStates; ++s) dst[kOffG + s] = second[kOffG + first[kOffG + s]];
-  if (AK == 4) {
-#pragma unroll 1
-    for (int s = 0; s < QChan<4>::kStates; ++s) dst[kOffA + s] = second[kOffA + first[kOffA + s]];
-  } else if (AK == 1) {
-    dst[kOffA] = uint8_t((first[kOffA] + second[kOffA]) % 255);
-  }
-}
-
-// Apply a table record to packed start states (r | g<<8 | b<<16 | a<<24).
-template <int AK>
-__device__ __forceinline__ uint32_t apply(const uint8_t* t, uint32_t st) {
-  uint32_t r = t[kOffR + (st & 0xFF)];
-  uint32_t g = t[kOffG + ((st >> 8) & 0xFF)];
-  uint32_t b = t[kOffB + ((st >> 16) & 0xFF)];
-  uint32_t a = 0;
-  if (AK == 4) a = t[kOffA + (st >> 24)];
-  if (AK == 1) a = ((st >> 24) + t[kOffA]) % 255;
-  return r | (g << 8) | (b << 16) | (a << 24);
-}
-
-template <int AK>
-__device__ __forceinline__ uint32_t initial_state() {
-  // zero carried error in every chain
-  return uint32_t(QChan<3>::kOff) | (uint32_t(QChan<2>::kOff) << 8) | (uint32_t(QChan<3>::kOff) << 16) |
-         (uint32_t(AK == 4 ? QChan<4>::kOff : AK == 1 ? 127 : 0) << 24);
-}
-
-template <int AK>
-__device__ __forceinline__ void identity(uint8_t* t) {
-  for (int s = 0; s < QChan<3>::kStates; ++s) t[kOffR + s] = t[kOffB + s] = uint8_t(s);
-  for (int s = 0; s < QChan<2>::kStates; ++s) t[kOffG + s] = uint8_t(s);
-  if (AK == 4)
-    for (int s = 0; s < QChan<4>::kStates; ++s) t[kOffA + s] = uint8_t(s);
-  if (AK == 1) t[kOffA] = 0;
-}
-
-// ---------------------------------------------------------------- SWAR step
+// ------------------------------------------------------------- SWAR steps
 // For a channel quantised with shift k (k = 3: 5 bits, k = 2: 6 bits) let
 // E = 2^k - 1 be the largest carried error, e = d + E in [0, 2E] the state and
 // src = 2^k q + r.  With t = r + e and s = src + d = 2^k q + t - E, qstep gives
@@ -130,37 +64,298 @@ __device__ __forceinline__ void identity(uint8_t* t) {
 // most two values), e' = t when s < 0 (q = 0, t < E) and e' = t - E when
 // s > 255 (q = maxv, t > 2E).  Both clamps are the middle formula plus or
 // minus 2^k + 1, selected by [t >= T].  Every byte of a word holds one state
-// biased by 16, so no lane ever borrows from its neighbour, and one step is
-//   t = ub + rm; m = (t + 1) & E; g = ((t + 128 - T) >> 7) & 1; ub' = g*j1 + m + bc
-// with per-source-byte constants rm, kk = 128 - T, bc, j1 (SwarConst).
-
-struct SwarConst {
-  uint32_t rm, kk, bc, j1;
-};
-
+// biased by 16, so no lane ever borrows from its neighbour.  With
+// t1 = ub + r - 15 (per byte) one step is
+//   m = t1 & E;  g = ((t1 + 127 - T) >> 7) & 1;  ub' = g*j1 + m + (16 + E - base - L)
+// where L = 2^k + 1 for q = 0 (else 0), H likewise for q = maxv and
+// j1 = H + L - 1.  The q-dependent constants live in a shared table of one
+// word per q: byte 0 = 127 - T, byte 1 = 16 + E - base - L, byte 3 = j1.
 template <int K>
-__device__ __forceinline__ uint4 swar_const(int src) {
+__host__ __device__ __forceinline__ uint32_t swar_table_word(int q) {
   constexpr int E = (1 << K) - 1, maxv = 255 >> K;
-  const int r = src & E, q = src >> K;
   const int base = ((1 << K) * q - E) >> (8 - K);
   const int T = (1 << (8 - K)) * (base + 1) - ((1 << K) * q - E);
   const int L = q == 0 ? (1 << K) + 1 : 0, H = q == maxv ? (1 << K) + 1 : 0;
-  return make_uint4(uint32_t(r) * 0x01010101u - 0x10101010u, uint32_t(128 - T) * 0x01010101u,
-                    uint32_t(16 + E - base - L) * 0x01010101u, uint32_t(H + L - 1));
+  return uint32_t(127 - T) | (uint32_t(16 + E - base - L) << 8) | (uint32_t(H + L - 1) << 24);
+}
+
+struct SwarC {
+  uint32_t rm1, kk1, bc;
+  int j1;
+};
+
+template <int K>
+__device__ __forceinline__ SwarC swar_c(int src, const uint32_t* tab) {
+  constexpr uint32_t E = (1u << K) - 1;
+  const uint32_t tw = tab[src >> K];
+  SwarC c;
+  c.rm1 = (uint32_t(src) & E) * 0x01010101u - 0x0F0F0F0Fu;
+  c.kk1 = __byte_perm(tw, 0, 0x0000);
+  c.bc = __byte_perm(tw, 0, 0x1111);
+  c.j1 = int(tw) >> 24;
+  return c;
 }
 
 template <int K>
-__device__ __forceinline__ uint32_t swar_step(uint32_t ub, const uint4& c) {
-  constexpr uint32_t MASK = uint32_t((1 << K) - 1) * 0x01010101u;
-  const uint32_t t = ub + c.x;
-  const uint32_t m = (t + 0x01010101u) & MASK;
-  const uint32_t g = ((t + c.y) >> 7) & 0x01010101u;
-  return g * c.w + (m + c.z);
+__device__ __forceinline__ uint32_t swar_step(uint32_t ub, const SwarC& c) {
+  constexpr uint32_t MASK = ((1u << K) - 1) * 0x01010101u;
+  const uint32_t t1 = ub + c.rm1;
+  const uint32_t m = t1 & MASK;
+  const uint32_t g = ((t1 + c.kk1) >> 7) & 0x01010101u;
+  return g * uint32_t(c.j1) + (m + c.bc);
 }
 
-// Unpack SWAR words (states biased by 16) into a byte table.
-__device__ __forceinline__ void swar_store(const uint32_t* w, int nstates, uint8_t* out) {
-  for (int s = 0; s < nstates; ++s) out[s] = uint8_t(((w[s >> 2] >> (8 * (s & 3))) & 0xFF) - 16);
+// 4-bit alpha (k = 4, 31 states): t = e + r takes up to 46 values, so
+// s >> 4 takes up to three.  With src = 16 Q + r and states biased by 16,
+//   e' = t + A - 17 ([t >= 15] m15 + [t >= 31] m31)
+// where A = 17 - Q (0 for Q = 0, 2 for Q = 15), m15 = [Q > 0], m31 = [Q < 15]
+// (the clamps at Q = 0 and Q = 15 drop one of the two corrections).  Shared
+// table word per Q: byte 0 = A, byte 1 = m15, byte 2 = m31.
+__host__ __device__ __forceinline__ uint32_t swar4_table_word(int Q) {
+  const int A = Q == 15 ? 2 : Q == 0 ? 0 : 17 - Q;
+  return uint32_t(A) | (uint32_t(Q > 0) << 8) | (uint32_t(Q < 15) << 16);
+}
+
+struct Swar4C {
+  uint32_t r, a, m15, m31;
+};
+
+__device__ __forceinline__ Swar4C swar4_c(int src, const uint32_t* tab) {
+  const uint32_t tw = tab[src >> 4];
+  Swar4C c;
+  c.r = (uint32_t(src) & 15u) * 0x01010101u;
+  c.a = __byte_perm(tw, 0, 0x0000);
+  c.m15 = __byte_perm(tw, 0, 0x1111);
+  c.m31 = __byte_perm(tw, 0, 0x2222);
+  return c;
+}
+
+__device__ __forceinline__ uint32_t swar_step4(uint32_t u, const Swar4C& c) {
+  const uint32_t t = u + c.r;
+  const uint32_t g15 = ((t + 0x61616161u) >> 7) & c.m15;  // 128 - 15 - 16 = 97
+  const uint32_t g31 = ((t + 0x51515151u) >> 7) & c.m31;  // 128 - 31 - 16 = 81
+  return (t + c.a) - 17u * (g15 + g31);
+}
+
+// ------------------------------------------------------------------ records
+// The end state of each chain for every start state, one byte per state
+// (states unbiased: red/blue 0..14, green 0..6, 4-bit alpha 0..30; the last
+// byte of each channel is a padding state that always holds a valid state).
+// For the 1-bit alpha chain a[0] is the sum of sources mod 255.
+struct Rec {
+  uint32_t r[4], g[2], b[4], a[8];
+};
+
+template <int AK>
+__device__ __forceinline__ void rec_identity(Rec& x) {
+  x.r[0] = x.b[0] = 0x03020100u;
+  x.r[1] = x.b[1] = 0x07060504u;
+  x.r[2] = x.b[2] = 0x0B0A0908u;
+  x.r[3] = x.b[3] = 0x070E0D0Cu;
+  x.g[0] = 0x03020100u;
+  x.g[1] = 0x03060504u;
+  if (AK == 4) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x.a[i] = 0x03020100u + 0x04040404u * uint32_t(i);
+    x.a[7] = 0x0F1E1D1Cu;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x.a[i] = 0;
+  }
+}
+
+// prmt selector from the low three bits of four byte indices.
+__device__ __forceinline__ uint32_t sel3(uint32_t idx) {
+  const uint32_t x = idx & 0x07070707u;
+  return __byte_perm(x | (x >> 4), 0, 0x0020);
+}
+
+__device__ __forceinline__ uint32_t bytemask(uint32_t idx, int bit) {
+  return ((idx >> bit) & 0x01010101u) * 0xFFu;
+}
+
+// g[idx[i]] for four byte indices below 8, 16 or 32.
+__device__ __forceinline__ uint32_t gather8(const uint32_t* g, uint32_t idx) {
+  return __byte_perm(g[0], g[1], sel3(idx));
+}
+__device__ __forceinline__ uint32_t gather16(const uint32_t* g, uint32_t idx) {
+  const uint32_t s = sel3(idx);
+  const uint32_t lo = __byte_perm(g[0], g[1], s), hi = __byte_perm(g[2], g[3], s);
+  const uint32_t m = bytemask(idx, 3);
+  return (hi & m) | (lo & ~m);
+}
+__device__ __forceinline__ uint32_t gather32(const uint32_t* g, uint32_t idx) {
+  const uint32_t s = sel3(idx);
+  const uint32_t p0 = __byte_perm(g[0], g[1], s), p1 = __byte_perm(g[2], g[3], s);
+  const uint32_t p2 = __byte_perm(g[4], g[5], s), p3 = __byte_perm(g[6], g[7], s);
+  const uint32_t m3 = bytemask(idx, 3), m4 = bytemask(idx, 4);
+  const uint32_t lo = (p1 & m3) | (p0 & ~m3), hi = (p3 & m3) | (p2 & ~m3);
+  return (hi & m4) | (lo & ~m4);
+}
+
+// out = `first`, then `second`.
+template <int AK>
+__device__ __forceinline__ Rec compose(const Rec& first, const Rec& second) {
+  Rec o;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    o.r[i] = gather16(second.r, first.r[i]);
+    o.b[i] = gather16(second.b, first.b[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) o.g[i] = gather8(second.g, first.g[i]);
+  if (AK == 4) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) o.a[i] = gather32(second.a, first.a[i]);
+  } else if (AK == 1) {
+    o.a[0] = (first.a[0] + second.a[0]) % 255u;
+#pragma unroll
+    for (int i = 1; i < 8; ++i) o.a[i] = 0;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) o.a[i] = 0;
+  }
+  return o;
+}
+
+// Packed chain states: r | g << 8 | b << 16 | a << 24 (alpha: 4-bit state, or
+// (carried error + 127) for the 1-bit chain).
+template <int AK>
+__device__ __forceinline__ uint32_t apply(const Rec& t, uint32_t st) {
+  const uint32_t r = gather16(t.r, st & 0xFFu) & 0xFFu;
+  const uint32_t g = gather8(t.g, (st >> 8) & 0xFFu) & 0xFFu;
+  const uint32_t b = gather16(t.b, (st >> 16) & 0xFFu) & 0xFFu;
+  uint32_t a = 0;
+  if (AK == 4) a = gather32(t.a, st >> 24) & 0xFFu;
+  if (AK == 1) a = ((st >> 24) + t.a[0]) % 255u;
+  return r | (g << 8) | (b << 16) | (a << 24);
+}
+
+template <int AK>
+__device__ __forceinline__ uint32_t initial_state() {
+  // zero carried error in every chain
+  return 7u | (3u << 8) | (7u << 16) | (uint32_t(AK == 4 ? 15 : AK == 1 ? 127 : 0) << 24);
+}
+
+template <int AK>
+__device__ __forceinline__ Rec shfl_up_rec(const Rec& x, int d) {
+  Rec o;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    o.r[i] = __shfl_up_sync(0xFFFFFFFFu, x.r[i], d);
+    o.b[i] = __shfl_up_sync(0xFFFFFFFFu, x.b[i], d);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) o.g[i] = __shfl_up_sync(0xFFFFFFFFu, x.g[i], d);
+  if (AK == 4) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) o.a[i] = __shfl_up_sync(0xFFFFFFFFu, x.a[i], d);
+  } else if (AK == 1) {
+    o.a[0] = __shfl_up_sync(0xFFFFFFFFu, x.a[0], d);
+  }
+  return o;
+}
+
+__device__ __forceinline__ void rec_store(uint32_t* p, const Rec& x) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) p[i] = x.r[i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) p[4 + i] = x.g[i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) p[6 + i] = x.b[i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) p[10 + i] = x.a[i];
+}
+
+__device__ __forceinline__ Rec rec_load(const uint32_t* p) {
+  Rec x;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) x.r[i] = p[i];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) x.g[i] = p[4 + i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) x.b[i] = p[6 + i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x.a[i] = p[10 + i];
+  return x;
+}
+
+// Global aggregate records are read after an acquire of their status word;
+// L2 loads (no L1) keep them coherent.
+__device__ __forceinline__ Rec rec_load_global(const uint32_t* p) {
+  Rec x;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) x.r[i] = __ldcg(p + i);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) x.g[i] = __ldcg(p + 4 + i);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) x.b[i] = __ldcg(p + 6 + i);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x.a[i] = __ldcg(p + 10 + i);
+  return x;
+}
+
+// --------------------------------------------------------------- tile I/O
+
+struct TileSmem {
+  uint32_t px[kTile];               // RGBA words in, 5:6:5 words out
+  uint32_t tab3[32], tab2[64], tab4[16];
+  uint32_t wagg[kWarps][kRecWords];  // warps' inclusive records
+  uint32_t wstart[kWarps];           // warps' start states
+  uint32_t carry;
+};
+
+// Texels [p0, p0 + n) of `it` into px[0, n) as RGBA words (alpha 0 for RGB).
+__device__ __forceinline__ void load_tile(const DitherItem& it, long long p0, int n, uint32_t* px) {
+  const int t = threadIdx.x;
+  if (it.srccomps == 4) {
+    const uint8_t* s = it.src + p0 * 4;
+    int done = 0;
+    if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
+      const uint4* v = reinterpret_cast<const uint4*>(s);
+      for (int i = t; i < (n >> 2); i += kThreads) reinterpret_cast<uint4*>(px)[i] = __ldg(v + i);
+      done = n & ~3;
+    } else if ((reinterpret_cast<uintptr_t>(s) & 3) == 0) {
+      const uint32_t* v = reinterpret_cast<const uint32_t*>(s);
+      for (int i = t; i < n; i += kThreads) px[i] = __ldg(v + i);
+      done = n;
+    }
+    for (int i = done + t; i < n; i += kThreads) {
+      const uint8_t* b = s + 4 * i;
+      px[i] = uint32_t(b[0]) | (uint32_t(b[1]) << 8) | (uint32_t(b[2]) << 16) | (uint32_t(b[3]) << 24);
+    }
+  } else {
+    const uint8_t* s = it.src + p0 * 3;
+    int done = 0;
+    if ((reinterpret_cast<uintptr_t>(s) & 3) == 0) {
+      // four texels = three words
+      const uint32_t* v = reinterpret_cast<const uint32_t*>(s);
+      for (int i = t; i < (n >> 2); i += kThreads) {
+        const uint32_t w0 = __ldg(v + 3 * i), w1 = __ldg(v + 3 * i + 1), w2 = __ldg(v + 3 * i + 2);
+        reinterpret_cast<uint4*>(px)[i] =
+            make_uint4(w0 & 0xFFFFFFu, __funnelshift_r(w0, w1, 24) & 0xFFFFFFu,
+                       __funnelshift_r(w1, w2, 16) & 0xFFFFFFu, w2 >> 8);
+      }
+      done = n & ~3;
+    }
+    for (int i = done + t; i < n; i += kThreads) {
+      const uint8_t* b = s + 3 * i;
+      px[i] = uint32_t(b[0]) | (uint32_t(b[1]) << 8) | (uint32_t(b[2]) << 16);
+    }
+  }
+}
+
+// px[0, n) out to dst[p0, p0 + n).
+__device__ __forceinline__ void store_tile(uint32_t* dst, long long p0, int n, const uint32_t* px) {
+  const int t = threadIdx.x;
+  uint32_t* d = dst + p0;
+  int done = 0;
+  if ((reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+    for (int i = t; i < (n >> 2); i += kThreads)
+      reinterpret_cast<uint4*>(d)[i] = reinterpret_cast<const uint4*>(px)[i];
+    done = n & ~3;
+  }
+  for (int i = done + t; i < n; i += kThreads) d[i] = px[i];
 }
 
 using Status = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
@@ -168,194 +363,175 @@ constexpr unsigned long long kAggReady = 1ull << 32;
 constexpr unsigned long long kIncReady = 2ull << 32;
 constexpr int kSpinLimit = 1 << 22;
 
-// Texel k (0..3) of a group of four, as an RGBA word, from raw words `w`
-// (four texels = 16 bytes for RGBA, 12 bytes for RGB).
-template <int SC>
-__device__ __forceinline__ uint32_t texel_of(const uint32_t* w, int k) {
-  if (SC == 4) return w[k];
-  const int b0 = 3 * k;
-  const uint64_t pair = uint64_t(w[b0 >> 2]) | (uint64_t(w[min((b0 >> 2) + 1, 2)]) << 32);
-  return uint32_t(pair >> (8 * (b0 & 3))) & 0xFFFFFFu;
-}
-
-// Four texels [p, p + 4) of the image as RGBA words (alpha 0 for RGB input);
-// texels at or beyond npx read as 0 and must not be used.
-template <int SC>
-__device__ __forceinline__ void load4(const uint8_t* __restrict__ src, long long p, long long npx, uint32_t* px) {
-  const uint8_t* s = src + p * SC;
-  if (p + 4 <= npx && (reinterpret_cast<uintptr_t>(s) & 3) == 0) {
-    uint32_t w[4];
-    const uint32_t* v = reinterpret_cast<const uint32_t*>(s);
-#pragma unroll
-    for (int i = 0; i < SC; ++i) w[i] = __ldg(v + i);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) px[k] = texel_of<SC>(w, k);
-  } else {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      uint32_t v = 0;
-      if (p + k < npx) {
-        const uint8_t* t = s + k * SC;
-        v = uint32_t(t[0]) | (uint32_t(t[1]) << 8) | (uint32_t(t[2]) << 16);
-        if (SC == 4) v |= uint32_t(t[3]) << 24;
-      }
-      px[k] = v;
-    }
+// The state at the start of tile g of an image whose tile within the image
+// is `lt`, given the tile's aggregate; publishes the tile's own records.
+template <int AK>
+__device__ uint32_t look_back(const DitherWork& w, long long g, long long lt, const Rec& agg) {
+  Status st(w.status[g]);
+  if (lt == 0) {
+    const uint32_t carry = initial_state<AK>();
+    st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+    return carry;
   }
+  uint32_t* gagg = reinterpret_cast<uint32_t*>(w.aggs + g * kRec);
+  rec_store(gagg, agg);
+  st.store(kAggReady, cuda::memory_order_release);
+  // acc: state at the end of tile k -> state at the start of this tile; the
+  // image's first tile always publishes its inclusive state, so the walk
+  // never leaves the image
+  Rec acc;
+  rec_identity<AK>(acc);
+  uint32_t carry = initial_state<AK>();
+  for (long long k = g - 1;; --k) {
+    Status sk(w.status[k]);
+    unsigned long long v = sk.load(cuda::memory_order_acquire);
+    int spins = 0;
+    while ((v >> 32) == 0 && spins < kSpinLimit) {
+      __nanosleep(64);
+      v = sk.load(cuda::memory_order_acquire);
+      ++spins;
+    }
+    if ((v >> 32) == 0) {
+      atomicExch(w.error, 1);
+      break;
+    }
+    if ((v >> 32) == 2) {
+      carry = apply<AK>(acc, uint32_t(v));
+      break;
+    }
+    acc = compose<AK>(rec_load_global(reinterpret_cast<const uint32_t*>(w.aggs + k * kRec)), acc);
+  }
+  st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+  return carry;
 }
 
-// Shared memory of one SIMPLE-dither tile.
-struct TileSmem {
-  uint8_t tbl[2][kThreads][kRec];
-  uint4 c3[256], c2[256];
-  uint32_t carry;
-};
-
-// One SIMPLE-dither tile: texels [tile_in_image * kTile, +kTile) of `it`,
-// chained through the status words `status[tile - tile_in_image ...]`.
-// `g` is the tile's global index (status / aggregate slot).
-template <int SC, int AK>
-__device__ __forceinline__ void simple_tile(const DitherItem& it, long long tile_in_image, long long g,
+// One SIMPLE-dither tile: texels [lt * kTile, +n) of `it` (already in
+// sm.px), chained through the status words; `g` is the tile's global index.
+// On return sm.px holds the tile's 5:6:5 words.
+template <int AK>
+__device__ __forceinline__ void simple_tile(const DitherItem& it, long long lt, long long g, int n,
                                             const DitherWork& w, TileSmem& sm) {
-  const int t = threadIdx.x;
-  const long long npx = (long long)it.width * it.height;
-  const long long p0 = tile_in_image * kTile + (long long)t * kSeg;
-  const int nvalid = int(max(0ll, min((long long)kSeg, npx - p0)));
-  const int alpha_const = (1 << it.alphabits) - 1;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int k0 = t * kSeg;
+  const int cnt = max(0, min(kSeg, n - k0));
+  const uint32_t* px = sm.px + k0;
 
-  // segment tables: all start states at once, four per word
-  uint32_t wr[4] = {0x13121110u, 0x17161514u, 0x1B1A1918u, 0x171E1D1Cu};  // red states 0..14 (+pad)
-  uint32_t wb[4] = {0x13121110u, 0x17161514u, 0x1B1A1918u, 0x171E1D1Cu};  // blue
-  uint32_t wg[2] = {0x13121110u, 0x13161514u};                            // green states 0..6 (+pad)
-  int asum = 0;
-  uint8_t* mine = sm.tbl[0][t];
+  // the segment's records, all start states at once (states biased by 16)
+  Rec x;
+  x.r[0] = x.b[0] = 0x13121110u;
+  x.r[1] = x.b[1] = 0x17161514u;
+  x.r[2] = x.b[2] = 0x1B1A1918u;
+  x.r[3] = x.b[3] = 0x171E1D1Cu;
+  x.g[0] = 0x13121110u;
+  x.g[1] = 0x13161514u;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x.a[i] = AK == 4 ? 0x13121110u + 0x04040404u * uint32_t(i) : 0u;
+  if (AK == 4) x.a[7] = 0x1F2E2D2Cu;
+  uint32_t asum = 0;
+#pragma unroll 1
+  for (int k = 0; k < cnt; ++k) {
+    const uint32_t p = px[k];
+    const SwarC cr = swar_c<3>(int(p & 0xFFu), sm.tab3);
+    const SwarC cg = swar_c<2>(int((p >> 8) & 0xFFu), sm.tab2);
+    const SwarC cb = swar_c<3>(int((p >> 16) & 0xFFu), sm.tab3);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x.r[i] = swar_step<3>(x.r[i], cr);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) x.g[i] = swar_step<2>(x.g[i], cg);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x.b[i] = swar_step<3>(x.b[i], cb);
+    if (AK == 1) asum += p >> 24;
+    if (AK == 4) {
+      const Swar4C ca = swar4_c(int(p >> 24), sm.tab4);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) x.a[i] = swar_step4(x.a[i], ca);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    x.r[i] -= 0x10101010u;
+    x.b[i] -= 0x10101010u;
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) x.g[i] -= 0x10101010u;
   if (AK == 4) {
-    for (int s = 0; s < QChan<4>::kStates; ++s) mine[kOffA + s] = uint8_t(s);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x.a[i] -= 0x10101010u;
   }
-  for (int k0 = 0; k0 < nvalid; k0 += 4) {
-    uint32_t px[4];
-    load4<SC>(it.src, p0 + k0, npx, px);
+  if (AK == 1) x.a[0] = asum % 255u;
+
+  // inclusive scan over the warp's lanes
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (k0 + k < nvalid) {
-        const uint32_t p = px[k];
-        const uint4 cr = sm.c3[p & 0xFF], cg = sm.c2[(p >> 8) & 0xFF], cb = sm.c3[(p >> 16) & 0xFF];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) wr[i] = swar_step<3>(wr[i], cr);
-#pragma unroll
-        for (int i = 0; i < 2; ++i) wg[i] = swar_step<2>(wg[i], cg);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) wb[i] = swar_step<3>(wb[i], cb);
-        if (AK == 1) asum += int(p >> 24);
-        if (AK == 4) {
-          // 4-bit alpha: 31 states, stepped one by one
-          const int src = int(p >> 24);
-          for (int s = 0; s < QChan<4>::kStates; ++s) {
-            int d = int(mine[kOffA + s]) - QChan<4>::kOff;
-            qstep<4>(d, src);
-            mine[kOffA + s] = uint8_t(d + QChan<4>::kOff);
-          }
-        }
-      }
-    }
+  for (int d = 1; d < 32; d <<= 1) {
+    const Rec o = shfl_up_rec<AK>(x, d);
+    if (lane >= d) x = compose<AK>(o, x);
   }
-  swar_store(wr, QChan<3>::kStates, mine + kOffR);
-  swar_store(wg, QChan<2>::kStates, mine + kOffG);
-  swar_store(wb, QChan<3>::kStates, mine + kOffB);
-  if (AK == 1) mine[kOffA] = uint8_t(asum % 255);
+  if (lane == 31) rec_store(sm.wagg[warp], x);
   __syncthreads();
 
-  // inclusive scan of the tables across the CTA
-  int cur = 0;
-  for (int off = 1; off < kThreads; off <<= 1) {
-    if (t >= off) compose<AK>(sm.tbl[cur][t - off], sm.tbl[cur][t], sm.tbl[cur ^ 1][t]);
-    else
-      for (int i = 0; i < kRec; ++i) sm.tbl[cur ^ 1][t][i] = sm.tbl[cur][t][i];
-    __syncthreads();
-    cur ^= 1;
-  }
-
-  // chain the image's tiles: publish, look back, publish the inclusive state
-  if (t == 0) {
-    const uint8_t* agg = sm.tbl[cur][kThreads - 1];
-    Status st(w.status[g]);
-    uint32_t carry = initial_state<AK>();
-    if (tile_in_image == 0) {
-      st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
-    } else {
-      uint8_t* gagg = w.aggs + g * kRec;
-      for (int i = 0; i < kRec; ++i) gagg[i] = agg[i];
-      st.store(kAggReady, cuda::memory_order_release);
-      // acc: state at the end of tile k -> state at the start of this tile;
-      // the image's first tile always publishes its inclusive state, so the
-      // walk never leaves the image
-      uint8_t acc[kRec];
-      identity<AK>(acc);
-      long long k = g - 1;
-      for (;;) {
-        Status sk(w.status[k]);
-        unsigned long long v = sk.load(cuda::memory_order_acquire);
-        int spins = 0;
-        while ((v >> 32) == 0 && spins < kSpinLimit) {
-          __nanosleep(64);
-          v = sk.load(cuda::memory_order_acquire);
-          ++spins;
-        }
-        if ((v >> 32) == 0) {
-          atomicExch(w.error, 1);
-          break;
-        }
-        if ((v >> 32) == 2) {
-          carry = apply<AK>(acc, uint32_t(v));
-          break;
-        }
-        // acc := agg[k] then acc
-        uint8_t tmp[kRec];
-        compose<AK>(w.aggs + k * kRec, acc, tmp);
-        for (int i = 0; i < kRec; ++i) acc[i] = tmp[i];
-        --k;
-      }
-      st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+  // warp 0: scan the warps' records, chain the tile, start state of each warp
+  if (warp == 0) {
+    Rec y;
+    if (lane < kWarps) y = rec_load(sm.wagg[lane]);
+    else rec_identity<AK>(y);
+#pragma unroll
+    for (int d = 1; d < kWarps; d <<= 1) {
+      const Rec o = shfl_up_rec<AK>(y, d);
+      if (lane >= d) y = compose<AK>(o, y);
     }
-    sm.carry = carry;
+    // tile aggregate = lane kWarps-1's inclusive record
+    Rec agg;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      agg.r[i] = __shfl_sync(0xFFFFFFFFu, y.r[i], kWarps - 1);
+      agg.b[i] = __shfl_sync(0xFFFFFFFFu, y.b[i], kWarps - 1);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) agg.g[i] = __shfl_sync(0xFFFFFFFFu, y.g[i], kWarps - 1);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) agg.a[i] = __shfl_sync(0xFFFFFFFFu, y.a[i], kWarps - 1);
+    uint32_t carry = 0;
+    if (lane == 0) carry = look_back<AK>(w, g, lt, agg);
+    carry = __shfl_sync(0xFFFFFFFFu, carry, 0);
+    // start of warp l = end of warp l-1
+    const uint32_t end = apply<AK>(y, carry);
+    const uint32_t start = __shfl_up_sync(0xFFFFFFFFu, end, 1);
+    if (lane < kWarps) sm.wstart[lane] = lane == 0 ? carry : start;
   }
   __syncthreads();
 
-  // replay the segment from its exact start state
-  const uint32_t start = t == 0 ? sm.carry : apply<AK>(sm.tbl[cur][t - 1], sm.carry);
-  int dr = int(start & 0xFF) - QChan<3>::kOff;
-  int dg = int((start >> 8) & 0xFF) - QChan<2>::kOff;
-  int db = int((start >> 16) & 0xFF) - QChan<3>::kOff;
-  int da = AK == 4 ? int(start >> 24) - QChan<4>::kOff : int(start >> 24) - 127;
-  uint32_t* o = it.dst + p0;
-  for (int k0 = 0; k0 < nvalid; k0 += 4) {
-    uint32_t px[4], out[4];
-    load4<SC>(it.src, p0 + k0, npx, px);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint32_t p = px[k];
-      uint32_t q = uint32_t(qstep<3>(dr, chan_of(p, 0))) | (uint32_t(qstep<2>(dg, chan_of(p, 1))) << 8) |
-                   (uint32_t(qstep<3>(db, chan_of(p, 2))) << 16);
-      uint32_t qa;
-      if (AK == 4) {
-        qa = uint32_t(qstep<4>(da, chan_of(p, 3)));
-      } else if (AK == 1) {
-        // diffuse1 (s2tc_algorithm.cpp:1208-1216)
-        const int v = chan_of(p, 3) + da;
-        qa = v >= 128;
-        da = v - (qa ? 255 : 0);
-      } else if (AK == 8) {
-        qa = uint32_t(chan_of(p, 3));
-      } else {
-        qa = uint32_t(alpha_const);
-      }
-      out[k] = q | (qa << 24);
-    }
-    if (k0 + 4 <= nvalid && (reinterpret_cast<uintptr_t>(o + k0) & 15) == 0) {
-      *reinterpret_cast<uint4*>(o + k0) = make_uint4(out[0], out[1], out[2], out[3]);
+  // the lane's start state: end of the previous lane
+  const uint32_t ws = sm.wstart[warp];
+  const uint32_t end = apply<AK>(x, ws);
+  uint32_t st = __shfl_up_sync(0xFFFFFFFFu, end, 1);
+  if (lane == 0) st = ws;
+
+  // replay the segment from its exact start state, in place
+  int dr = int(st & 0xFFu) - 7;
+  int dg = int((st >> 8) & 0xFFu) - 3;
+  int db = int((st >> 16) & 0xFFu) - 7;
+  int da = AK == 4 ? int(st >> 24) - 15 : int(st >> 24) - 127;
+  const uint32_t alpha_const = uint32_t((1 << it.alphabits) - 1);
+  uint32_t* o = sm.px + k0;
+#pragma unroll 1
+  for (int k = 0; k < cnt; ++k) {
+    const uint32_t p = o[k];
+    uint32_t q = uint32_t(qstep<3>(dr, int(p & 0xFFu))) | (uint32_t(qstep<2>(dg, int((p >> 8) & 0xFFu))) << 8) |
+                 (uint32_t(qstep<3>(db, int((p >> 16) & 0xFFu))) << 16);
+    uint32_t qa;
+    if (AK == 4) {
+      qa = uint32_t(qstep<4>(da, int(p >> 24)));
+    } else if (AK == 1) {
+      // diffuse1 (s2tc_algorithm.cpp:1208-1216)
+      const int v = int(p >> 24) + da;
+      qa = v >= 128;
+      da = v - (qa ? 255 : 0);
+    } else if (AK == 8) {
+      qa = p >> 24;
     } else {
-      for (int k = 0; k < min(4, nvalid - k0); ++k) o[k0 + k] = out[k];
+      qa = alpha_const;
     }
+    o[k] = q | (qa << 24);
   }
 }
 
@@ -374,44 +550,69 @@ __device__ __forceinline__ int tile_item(const DitherWork& w, long long g) {
 // DITHER_SIMPLE over every tile of every image of the work list.  Tiles take
 // tickets in launch order, so a tile only ever waits on tiles that started
 // before it.
-__global__ void __launch_bounds__(kThreads) k_dither_simple(DitherWork w) {
-  __shared__ TileSmem sm;
+#ifndef S2TC_DITHER_MINBLOCKS
+#define S2TC_DITHER_MINBLOCKS 3
+#endif
+__global__ void __launch_bounds__(kThreads, S2TC_DITHER_MINBLOCKS) k_dither_simple(DitherWork w) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem& sm = *reinterpret_cast<TileSmem*>(smem_raw);
   __shared__ unsigned int s_ticket;
   const int t = threadIdx.x;
-  sm.c3[t] = swar_const<3>(t);
-  sm.c2[t] = swar_const<2>(t);
+  if (t < 32) sm.tab3[t] = swar_table_word<3>(t);
+  if (t < 64) sm.tab2[t] = swar_table_word<2>(t);
+  if (t < 16) sm.tab4[t] = swar4_table_word(t);
   if (t == 0) s_ticket = atomicAdd(w.ticket, 1u);
   __syncthreads();
   const long long g = s_ticket;
   if (g >= w.total_tiles) return;
   const int item = tile_item(w, g);
-  const DitherItem it = w.items ? w.items[item] : w.single;
+  DitherItem it = w.single;
+  if (w.items) it = w.items[item];
   const long long lt = w.items ? g - __ldg(w.tile_offsets + item) : g;
-  if (it.srccomps == 3) simple_tile<3, 0>(it, lt, g, w, sm);
-  else if (it.alphabits == 1) simple_tile<4, 1>(it, lt, g, w, sm);
-  else if (it.alphabits == 4) simple_tile<4, 4>(it, lt, g, w, sm);
-  else simple_tile<4, 8>(it, lt, g, w, sm);
+  const long long npx = (long long)it.width * it.height;
+  const long long p0 = lt * kTile;
+  const int n = int(min((long long)kTile, npx - p0));
+  load_tile(it, p0, n, sm.px);
+  __syncthreads();
+  if (it.srccomps == 3) simple_tile<0>(it, lt, g, n, w, sm);
+  else if (it.alphabits == 1) simple_tile<1>(it, lt, g, n, w, sm);
+  else if (it.alphabits == 4) simple_tile<4>(it, lt, g, n, w, sm);
+  else simple_tile<8>(it, lt, g, n, w, sm);
+  __syncthreads();
+  store_tile(it.dst, p0, n, sm.px);
 }
 
 // DITHER_NONE (s2tc_algorithm.cpp:1269-1305): plain truncation, one tile per CTA.
 __global__ void __launch_bounds__(kThreads) k_dither_none(DitherWork w) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* px = reinterpret_cast<uint32_t*>(smem_raw);
   const long long g = blockIdx.x;
   if (g >= w.total_tiles) return;
   const int item = tile_item(w, g);
-  const DitherItem it = w.items ? w.items[item] : w.single;
+  DitherItem it = w.single;
+  if (w.items) it = w.items[item];
   const long long npx = (long long)it.width * it.height;
-  const long long base = (w.items ? g - __ldg(w.tile_offsets + item) : g) * kTile;
-  const int sc = it.srccomps == 3 ? 3 : 4;
+  const long long p0 = (w.items ? g - __ldg(w.tile_offsets + item) : g) * kTile;
+  const int n = int(min((long long)kTile, npx - p0));
+  load_tile(it, p0, n, px);
+  __syncthreads();
   const uint32_t ac = uint32_t((1 << it.alphabits) - 1);
-  for (long long p = base + threadIdx.x; p < min(npx, base + kTile); p += kThreads) {
-    const uint8_t* s = it.src + p * sc;
-    const uint32_t r = s[0] >> 3, gg = s[1] >> 2, b = s[2] >> 3;
-    const uint32_t al = sc == 4 ? uint32_t(s[3] >> (8 - it.alphabits)) : ac;
-    it.dst[p] = r | (gg << 8) | (b << 16) | (al << 24);
+  const int ash = 8 - it.alphabits;
+  const bool rgb = it.srccomps == 3;
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    const uint32_t p = px[i];
+    const uint32_t al = rgb ? ac : (p >> 24) >> ash;
+    px[i] = ((p & 0xFFu) >> 3) | ((((p >> 8) & 0xFFu) >> 2) << 8) | ((((p >> 16) & 0xFFu) >> 3) << 16) | (al << 24);
   }
+  __syncthreads();
+  store_tile(it.dst, p0, n, px);
 }
 
 std::atomic<long long> g_launches{0};
+
+cudaError_t set_smem(const void* fn, size_t bytes) {
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+}
 
 }  // namespace
 
@@ -421,7 +622,7 @@ long long launches_so_far() { return g_launches.load(std::memory_order_relaxed);
 long long dither_tile_texels() { return kTile; }
 
 size_t dither_batch_scratch_bytes(long long tiles) {
-  // status words, aggregate tables, ticket (plus alignment slack)
+  // status words, aggregate records, ticket (plus alignment slack)
   return size_t(tiles) * (sizeof(unsigned long long) + kRec) + 256;
 }
 
@@ -429,9 +630,16 @@ size_t dither_scratch_bytes(long long npx) { return dither_batch_scratch_bytes((
 
 cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cudaStream_t s) {
   if (w.total_tiles <= 0) return cudaSuccess;
+  // the attribute is set once per process (the first call on any device)
+  static const cudaError_t attr = [] {
+    cudaError_t e = set_smem(reinterpret_cast<const void*>(k_dither_simple), sizeof(TileSmem));
+    if (e == cudaSuccess) e = set_smem(reinterpret_cast<const void*>(k_dither_none), kTile * sizeof(uint32_t));
+    return e;
+  }();
+  if (attr != cudaSuccess) return attr;
   if (dither == DI_NONE) {
     count_launches(1);
-    k_dither_none<<<unsigned(w.total_tiles), kThreads, 0, s>>>(w);
+    k_dither_none<<<unsigned(w.total_tiles), kThreads, kTile * sizeof(uint32_t), s>>>(w);
     return cudaGetLastError();
   }
   w.status = reinterpret_cast<unsigned long long*>(scratch);
@@ -443,7 +651,7 @@ cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cuda
   e = cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   count_launches(1);
-  k_dither_simple<<<unsigned(w.total_tiles), kThreads, 0, s>>>(w);
+  k_dither_simple<<<unsigned(w.total_tiles), kThreads, sizeof(TileSmem), s>>>(w);
   return cudaGetLastError();
 }
 
