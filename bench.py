@@ -59,6 +59,11 @@ WORKLOADS = {
     # mixed DXT1/DXT3/DXT5, RGB8/RGBA8: one batched graph launch per step
     "mip_chains_256_wavg_rand64_always": dict(
         w=0, h=0, sc=0, fmt=0, dither=1, metric=5, nrandom=64, refine=1, gen="mips", seed=3, count=256),
+    # 64 RGB8 normal maps of 2048x2048 (16 distinct maps, each used four
+    # times) in one batched graph launch
+    "normal_maps_64x2048_dxt1_normalmap_rand64_loop": dict(
+        w=2048, h=2048, sc=3, fmt=0x83F1, dither=1, metric=7, nrandom=64, refine=2, gen="normal_batch", seed=4,
+        count=64, distinct=16),
     # requests of log-uniform size 64..4096, DXT1/DXT5, WAVG/SRGB_MIXED/NORMALMAP,
     # through the continuous-batching request loop under a 32 GB budget; a
     # step is 1000 requests
@@ -92,6 +97,11 @@ def algorithmic_bytes_per_texel(wl: dict) -> float:
 
 def config_dict(wl_name: str, wl: dict) -> dict:
     import s2tc_gb300 as s2
+    if wl["gen"] == "normal_batch":
+        return {"workload": wl_name, "maps": wl["count"], "distinct_maps": wl["distinct"], "width": wl["w"],
+                "height": wl["h"], "srccomps": 3, "format": "DXT1", "dither": s2.DITHER_NAMES[wl["dither"]],
+                "colordist": "NORMALMAP", "random_colors": wl["nrandom"], "refine": s2.REFINE_NAMES[wl["refine"]],
+                "l2": "the batch's inputs (805 MB) and rand words (13 GB) exceed the 129 MB L2"}
     if wl["gen"] == "serving":
         return {"workload": wl_name, "requests_per_step": wl["per_step"], "sizes": "log-uniform 64..4096 per side",
                 "formats": "DXT1/DXT5 uniform", "colordist": "WAVG/SRGB_MIXED/NORMALMAP uniform",
@@ -265,15 +275,20 @@ def cpu_baseline_port(wl_name: str, wl: dict, gpu_out0: np.ndarray | None) -> di
 # ------------------------------------------------------------ batch workload
 
 def run_batch_workload(args, wl_name: str, wl: dict) -> None:
-    """Uneven mip chains: the batched graph launch vs one s2tc_gpu_compress
-    per level, both with the same resident rand words."""
+    """Batched workloads (uneven mip chains, or many normal maps): one batched
+    graph launch vs one s2tc_gpu_compress per image, both with the same
+    resident rand words."""
     import torch
     import s2tc_gb300 as s2
     from s2tc_gb300 import workloads
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    tex = workloads.mip_textures(wl["seed"], count=wl["count"], lo=4, hi=2048)
     opt = s2.options(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
-    levels = [(t, lvl) for t in tex for lvl in t["levels"]]
+    if wl["gen"] == "mips":
+        tex = workloads.mip_textures(wl["seed"], count=wl["count"], lo=4, hi=2048)
+        levels = [(t, lvl) for t in tex for lvl in t["levels"]]
+    else:
+        maps = [workloads.normal_map(wl["seed"] + i, wl["w"], wl["h"]) for i in range(wl["distinct"])]
+        levels = [({"fmt": wl["fmt"], "srccomps": 3}, maps[i % wl["distinct"]]) for i in range(wl["count"])]
     gen = torch.Generator(device="cuda")
     gen.manual_seed(11)
     images, host_src, host_rand = [], [], []
@@ -350,15 +365,21 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
 
     cpu = None
     if not args.no_cpu_baseline:
-        # the CPU port on a bounded sample: the first levels until ~1.5 M texels
+        # the CPU port on a bounded sample: the first levels until ~1.5 M
+        # texels (a band of rows of the first image when that alone is larger)
         sys.path.insert(0, str(ROOT / "oracle"))
         import pyoracle
         oracle = pyoracle.Oracle()
         sample, sample_tex = [], 0
         for t, lvl in levels:
+            if not sample and lvl.shape[0] * lvl.shape[1] > 1_500_000:
+                rows = max(4, (1_000_000 // lvl.shape[1]) & ~3)
+                sample.append((t, np.ascontiguousarray(lvl[:rows])))
+                sample_tex = rows * lvl.shape[1]
+                break
             sample.append((t, lvl))
             sample_tex += lvl.shape[0] * lvl.shape[1]
-            if sample_tex >= 1_500_000:
+            if sample_tex >= 1_000_000:
                 break
         pyoracle.srand(1)
         c0 = time.perf_counter()
@@ -368,7 +389,8 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
                             wl["nrandom"], wl["refine"])
         dt = time.perf_counter() - c0
         cpu = {"value": sample_tex / dt, "unit": "texels/s", "cores": 1, "kind": "port",
-               "sample": f"the first {len(sample)} levels ({sample_tex} texels), single thread ({dt:.2f} s)"}
+               "sample": f"the first {len(sample)} images (a band of rows when the first is large; {sample_tex} texels), "
+                          f"single thread ({dt:.2f} s)"}
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -587,12 +609,12 @@ def main() -> None:
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
-        if wl["gen"] in ("mips", "serving"):
+        if wl["gen"] in ("mips", "serving", "normal_batch"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times single-image workloads"}))
             return
         run_reference_arm(args, args.workload, wl)
         return
-    if wl["gen"] == "mips":
+    if wl["gen"] in ("mips", "normal_batch"):
         run_batch_workload(args, args.workload, wl)
         return
     if wl["gen"] == "serving":

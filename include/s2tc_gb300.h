@@ -201,6 +201,53 @@ int s2tc_gpu_compress_noalloc(int srccomps, int width, int height, const void *d
 			      void *d_dst, long long dst_pitch, const s2tc_options *opt, const unsigned int *d_rand,
 			      void *stream);
 
+/* ---------------------------------------------------------------------
+ * Part 3: the reference's command-line tools, in memory, on the GPU.
+ * --------------------------------------------------------------------- */
+
+/* Bytes of the DDS file s2tc_compress writes for a width x height image in
+ * `format` (header + every mip level down to 1x1), or -1 for a bad format or
+ * size. */
+long long s2tc_dds_size(int width, int height, unsigned int format);
+
+/* s2tc_compress (s2tc_compress.c:594-719) from the RGBA8 buffer it builds
+ * after loading its TGA (s2tc_compress.c:634-639): writes the DDS file (128-
+ * byte header, then every mip level from `width` x `height` down to 1x1,
+ * Image_MipReduce32 box filter, s2tc_compress.c:426-493) into `out`, which
+ * must hold s2tc_dds_size bytes.  `format` is the GL enum the tool's `-t`
+ * selects (DXT1 = GL_COMPRESSED_RGBA_S3TC_DXT1_EXT).  `opt` NULL reads the
+ * S2TC_* environment like tx_compress_dxtn.  Levels are built and encoded on
+ * the GPU; rand() is drawn per level in order, as the tool's
+ * tx_compress_dxtn calls draw it. */
+int s2tc_compress_dds(const void *rgba, int width, int height, unsigned int format, const s2tc_options *opt,
+		      void *out, long long out_size, long long *written);
+
+/* Decode a whole image of S2TC/S3TC blocks (packed block rows) on the GPU
+ * with the semantics of fetch_2d_texel_rgb_dxt1 (format
+ * GL_COMPRESSED_RGB_S3TC_DXT1_EXT), _rgba_dxt1, _rgba_dxt3 and _rgba_dxt5
+ * (s2tc_libtxc_dxtn.cpp:35-140), including their checkerboard decode of
+ * indices 2 and 3.  Output: RGBA8 texels (BGRA8 when `bgra` is non-zero),
+ * rows `dst_pitch` bytes apart (0: width*4).  Asynchronous on `stream`. */
+int s2tc_gpu_decode(const void *d_blocks, unsigned int format, int width, int height, void *d_out,
+		    long long dst_pitch, int bgra, void *stream);
+
+/* s2tc_decompress (s2tc_decompress.c:156-207) in memory: the base level of a
+ * DXT1/DXT3/DXT5 DDS file as an uncompressed 32-bit TGA (18-byte header, BGRA
+ * rows top to bottom); `tga` must hold 18 + width*height*4 bytes.  Another
+ * FourCC prints the tool's message and returns S2TC_ERR_FORMAT. */
+int s2tc_decompress_dds(const void *dds, long long size, void *tga, long long tga_size, long long *written);
+
+/* s2tc_from_s3tc's per-block rewrite (s2tc_from_s3tc.cpp:77-190) of `nblocks`
+ * device-resident blocks of `format` (DXT1 blocks keep transparent texels;
+ * DXT3/DXT5 colour halves and DXT5 alpha halves are rewritten).  `d_src` may
+ * equal `d_dst`.  Asynchronous on `stream`. */
+int s2tc_gpu_from_s3tc(const void *d_src, void *d_dst, long long nblocks, unsigned int format, void *stream);
+
+/* s2tc_from_s3tc (s2tc_from_s3tc.cpp:209-269) in memory: copies the 128-byte
+ * header and converts every whole block after it (a trailing partial block is
+ * dropped, as the tool's read loop does).  `out` must hold `size` bytes. */
+int s2tc_from_s3tc_dds(const void *dds, long long size, void *out, long long out_size, long long *written);
+
 /* Text of the last error this thread saw (empty when none). */
 const char *s2tc_last_error(void);
 

@@ -73,6 +73,17 @@ class Oracle:
         lib.s2tc_oracle_color_dist.argtypes = [i] * 7
         lib.s2tc_oracle_color_dist.restype = ctypes.c_int32
         lib.s2tc_oracle_fetch.argtypes = [i, i, i, vp, i, i, vp]
+        lg = ctypes.c_long
+        lib.s2tc_oracle_mip_reduce.argtypes = [vp, vp, ctypes.POINTER(i), ctypes.POINTER(i)]
+        lib.s2tc_oracle_dds_size.argtypes = [i, i, u]
+        lib.s2tc_oracle_dds_size.restype = lg
+        lib.s2tc_oracle_dds.argtypes = [vp, i, i, u, i, i, i, i, vp]
+        lib.s2tc_oracle_dds.restype = lg
+        lib.s2tc_oracle_decompress.argtypes = [vp, vp]
+        lib.s2tc_oracle_decompress.restype = lg
+        lib.s2tc_oracle_from_s3tc_block.argtypes = [i, vp]
+        lib.s2tc_oracle_from_s3tc.argtypes = [vp, lg, vp]
+        lib.s2tc_oracle_from_s3tc.restype = lg
         self.lib = lib
 
     def compress(self, srccomps, w, h, src, fmt, dither, metric, nrandom, refine,
@@ -107,6 +118,83 @@ class Oracle:
         t = np.zeros(4, np.uint8)
         self.lib.s2tc_oracle_fetch(dxt, rgba_dxt1, stride, _vp(data), i, j, _vp(t))
         return t
+
+
+    # ---- the reference's command-line tools, in memory
+
+    def mip_reduce(self, rgba, w, h):
+        """One Image_MipReduce32 step towards 1x1: (pixels, w, h)."""
+        src = np.ascontiguousarray(rgba, dtype=np.uint8).reshape(-1)
+        out = np.zeros(max(1, (w // 2 or 1) * (h // 2 or 1)) * 4, np.uint8)
+        cw, ch = ctypes.c_int(w), ctypes.c_int(h)
+        self.lib.s2tc_oracle_mip_reduce(_vp(src), _vp(out), ctypes.byref(cw), ctypes.byref(ch))
+        return out[: cw.value * ch.value * 4], cw.value, ch.value
+
+    def dds_size(self, w, h, fmt) -> int:
+        return self.lib.s2tc_oracle_dds_size(w, h, fmt)
+
+    def dds(self, rgba, w, h, fmt, dither, metric, nrandom, refine, seed=None) -> bytes:
+        """s2tc_compress's DDS output for an RGBA8 image."""
+        src = np.ascontiguousarray(rgba, dtype=np.uint8).reshape(-1)
+        out = np.zeros(self.dds_size(w, h, fmt), np.uint8)
+        if seed is not None:
+            srand(seed)
+        n = self.lib.s2tc_oracle_dds(_vp(src), w, h, fmt, dither, metric, nrandom, refine, _vp(out))
+        assert n == out.size, (n, out.size)
+        return out.tobytes()
+
+    def decompress(self, dds: bytes) -> bytes:
+        """s2tc_decompress's TGA output for a DXT1/3/5 DDS file."""
+        src = np.frombuffer(dds, np.uint8).copy()
+        w, h = int.from_bytes(dds[16:20], "little"), int.from_bytes(dds[12:16], "little")
+        out = np.zeros(18 + 4 * w * h, np.uint8)
+        n = self.lib.s2tc_oracle_decompress(_vp(src), _vp(out))
+        if n < 0:
+            raise ValueError("unsupported FourCC")
+        return out[:n].tobytes()
+
+    def from_s3tc(self, dds: bytes) -> bytes:
+        """s2tc_from_s3tc's output for an S3TC DDS file."""
+        src = np.frombuffer(dds, np.uint8).copy()
+        out = np.zeros(max(128, len(dds)), np.uint8)
+        n = self.lib.s2tc_oracle_from_s3tc(_vp(src), len(dds), _vp(out))
+        if n < 0:
+            raise ValueError("unsupported file")
+        return out[:n].tobytes()
+
+    def from_s3tc_blocks(self, blocks: np.ndarray, dxt: int) -> np.ndarray:
+        out = np.ascontiguousarray(blocks, dtype=np.uint8).copy()
+        bs = 8 if dxt == 0 else 16
+        for k in range(out.size // bs):
+            self.lib.s2tc_oracle_from_s3tc_block(dxt, ctypes.c_void_p(out.ctypes.data + k * bs))
+        return out
+
+
+class ReferenceTools:
+    """The reference's s2tc_compress, s2tc_decompress and s2tc_from_s3tc
+    programs compiled from its own sources (`make -C oracle ref`)."""
+
+    def __init__(self, bindir: os.PathLike | None = None):
+        self.bindir = Path(bindir or REF_SO.parent)
+
+    def available(self) -> bool:
+        return all((self.bindir / t).exists() for t in ("s2tc_compress", "s2tc_decompress", "s2tc_from_s3tc"))
+
+    def _run(self, tool, args, data: bytes, env=None) -> bytes:
+        import subprocess
+        r = subprocess.run([str(self.bindir / tool), *args], input=data, capture_output=True, env=env, check=True)
+        return r.stdout
+
+    def compress(self, tga: bytes, fourcc: str, dither, metric, nrandom, refine) -> bytes:
+        env = dict(os.environ, S2TC_DITHER_MODE=DITHER_NAMES[dither], S2TC_COLORDIST_MODE=COLORDIST_NAMES[metric],
+                   S2TC_RANDOM_COLORS=str(nrandom), S2TC_REFINE_COLORS=REFINE_NAMES[refine])
+        return self._run("s2tc_compress", ["-t", fourcc], tga, env)
+
+    def decompress(self, dds: bytes) -> bytes:
+        return self._run("s2tc_decompress", [], dds)
+
+    def from_s3tc(self, dds: bytes) -> bytes:
+        return self._run("s2tc_from_s3tc", [], dds)
 
 
 class Reference:

@@ -762,17 +762,19 @@ int s2tc_oracle_format_dxt(unsigned int fmt)
 }
 
 /* tx_compress_dxtn with the knobs passed explicitly
- * (s2tc_libtxc_dxtn.cpp:142-299).  Returns 0, or -1 for a bad format (nothing
+ * (s2tc_libtxc_dxtn.cpp:142-299).  `prev_a1` carries the second alpha
+ * endpoint that the last block of the previous call left in the encoder's
+ * stack slot (-1: none, the first block duplicates its own alpha); on return
+ * it holds this call's leftover.  Returns 0, or -1 for a bad format (nothing
  * written). */
-int s2tc_oracle_compress(int srccomps, int width, int height, const uint8_t *src,
-			 unsigned int fmt, uint8_t *dest, int dst_row_stride,
-			 int dither, int metric, int nrandom, int refine)
+int s2tc_oracle_compress_ex(int srccomps, int width, int height, const uint8_t *src,
+			    unsigned int fmt, uint8_t *dest, int dst_row_stride,
+			    int dither, int metric, int nrandom, int refine, int *prev_a1)
 {
 	int dxt = s2tc_oracle_format_dxt(fmt);
 	int bs, i, j;
 	long row_diff;
 	uint8_t *t565, *o = dest;
-	int prev_a1 = -1;   /* a1 left behind by the previous block of this call */
 	if (dxt < 0) return -1;
 	t565 = (uint8_t *)malloc((size_t)width * height * 4 + 1);
 	s2tc_oracle_rgb565_image(t565, src, width, height, srccomps,
@@ -784,14 +786,23 @@ int s2tc_oracle_compress(int srccomps, int width, int height, const uint8_t *src
 		int bh = height > j + 3 ? 4 : height - j;
 		for (i = 0; i < width; i += 4) {
 			int bw = width > i + 3 ? 4 : width - i;
-			prev_a1 = s2tc_oracle_encode_block_ex(o, t565 + ((long)j * width + i) * 4, width,
-							      bw, bh, dxt, metric, nrandom, refine, prev_a1);
+			*prev_a1 = s2tc_oracle_encode_block_ex(o, t565 + ((long)j * width + i) * 4, width,
+							       bw, bh, dxt, metric, nrandom, refine, *prev_a1);
 			o += bs;
 		}
 		o += row_diff;
 	}
 	free(t565);
 	return 0;
+}
+
+int s2tc_oracle_compress(int srccomps, int width, int height, const uint8_t *src,
+			 unsigned int fmt, uint8_t *dest, int dst_row_stride,
+			 int dither, int metric, int nrandom, int refine)
+{
+	int prev_a1 = -1;
+	return s2tc_oracle_compress_ex(srccomps, width, height, src, fmt, dest, dst_row_stride,
+				       dither, metric, nrandom, refine, &prev_a1);
 }
 
 /* ---------------------------------------------------------- texel decoders */
@@ -837,4 +848,238 @@ void s2tc_oracle_fetch(int dxt, int rgba_dxt1, int stride, const uint8_t *data, 
 		else if (ab >= 2 && odd) a = a1;
 		t[3] = (uint8_t)a;
 	}
+}
+
+/* ------------------------------------------------------ command-line tools */
+/* The pipelines of the reference's three tools, with their file formats kept
+ * in memory: s2tc_compress (RGBA in, DDS with a full mip chain out),
+ * s2tc_decompress (DDS in, TGA out) and s2tc_from_s3tc (S3TC DDS in, S2TC DDS
+ * out).  Image loading (LoadTGA_BGRA) is left to the caller: the input here is
+ * the RGBA buffer that s2tc_compress.c:634-639 produces. */
+
+/* Image_MipReduce32 towards 1x1 (s2tc_compress.c:426-493), out of place: a
+ * dimension above 1 halves (rounding down, the odd last row/column is
+ * dropped); 2x2, 2x1 or 1x2 boxes average with a truncating shift. */
+void s2tc_oracle_mip_reduce(const uint8_t *in, uint8_t *out, int *width, int *height)
+{
+	int w = *width, h = *height, x, y, c;
+	long row = (long)w * 4;
+	if (w > 1) {
+		w >>= 1;
+		if (h > 1) {
+			h >>= 1;
+			for (y = 0; y < h; ++y)
+				for (x = 0; x < w; ++x)
+					for (c = 0; c < 4; ++c) {
+						const uint8_t *p = in + 2 * y * row + 8 * x + c;
+						out[((long)y * w + x) * 4 + c] = (uint8_t)((p[0] + p[4] + p[row] + p[row + 4]) >> 2);
+					}
+		} else {
+			for (y = 0; y < h; ++y)
+				for (x = 0; x < w; ++x)
+					for (c = 0; c < 4; ++c) {
+						const uint8_t *p = in + y * row + 8 * x + c;
+						out[((long)y * w + x) * 4 + c] = (uint8_t)((p[0] + p[4]) >> 1);
+					}
+		}
+	} else if (h > 1) {
+		h >>= 1;
+		for (y = 0; y < h; ++y)
+			for (x = 0; x < w; ++x)
+				for (c = 0; c < 4; ++c) {
+					const uint8_t *p = in + 2 * y * row + 4 * x + c;
+					out[((long)y * w + x) * 4 + c] = (uint8_t)((p[0] + p[row]) >> 1);
+				}
+	}
+	*width = w;
+	*height = h;
+}
+
+static void put32(uint8_t *p, uint32_t v)
+{
+	p[0] = (uint8_t)v; p[1] = (uint8_t)(v >> 8); p[2] = (uint8_t)(v >> 16); p[3] = (uint8_t)(v >> 24);
+}
+
+static uint32_t get32(const uint8_t *p)
+{
+	return p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+
+/* Bytes of the DDS file s2tc_compress writes for a width x height image. */
+long s2tc_oracle_dds_size(int width, int height, unsigned int fmt)
+{
+	int dxt = s2tc_oracle_format_dxt(fmt), w = width, h = height;
+	long n = 128, bs = dxt == S2TC_O_DXT1 ? 8 : 16;
+	if (dxt < 0 || width < 1 || height < 1) return -1;
+	for (;;) {
+		n += (long)((w + 3) / 4) * ((h + 3) / 4) * bs;
+		if (w == 1 && h == 1) break;
+		if (w > 1) w >>= 1;
+		if (h > 1) h >>= 1;
+	}
+	return n;
+}
+
+/* s2tc_compress's output for an RGBA image (s2tc_compress.c:641-719): the
+ * 128-byte DDS header (mip count, base level size, "alpha pixels" flag when any
+ * base texel has alpha != 255, FourCC), then every level from the base down to
+ * 1x1, each compressed like tx_compress_dxtn with packed block rows.  Returns
+ * the bytes written, or -1 for a bad format or size. */
+long s2tc_oracle_dds(const uint8_t *rgba, int width, int height, unsigned int fmt,
+		     int dither, int metric, int nrandom, int refine, uint8_t *out)
+{
+	int dxt = s2tc_oracle_format_dxt(fmt), mipcount = 0, w = width, h = height, alpha = 0;
+	int prev_a1 = -1;  /* the encoder's stack slot, carried from level to level */
+	long i, npx = (long)width * height, bs = dxt == S2TC_O_DXT1 ? 8 : 16;
+	uint8_t *pic, *next, *o;
+	if (dxt < 0 || width < 1 || height < 1) return -1;
+	while (width >= (1 << mipcount) || height >= (1 << mipcount)) ++mipcount;
+	for (i = 0; i < npx; ++i)
+		if (rgba[i * 4 + 3] != 255) { alpha = 1; break; }
+	memset(out, 0, 128);
+	memcpy(out, "DDS ", 4);
+	put32(out + 4, 0x7c);
+	put32(out + 8, 0x000a1007);
+	put32(out + 12, (uint32_t)height);
+	put32(out + 16, (uint32_t)width);
+	put32(out + 20, (uint32_t)(((width + 3) / 4) * ((height + 3) / 4) * bs));
+	put32(out + 28, (uint32_t)mipcount);
+	put32(out + 76, 0x20);
+	put32(out + 80, alpha ? 5 : 4);
+	memcpy(out + 84, dxt == S2TC_O_DXT1 ? "DXT1" : dxt == S2TC_O_DXT3 ? "DXT3" : "DXT5", 4);
+	put32(out + 108, 0x00401008);
+	o = out + 128;
+	pic = (uint8_t *)malloc((size_t)npx * 4 + 4);
+	next = (uint8_t *)malloc((size_t)npx * 4 + 4);
+	memcpy(pic, rgba, (size_t)npx * 4);
+	for (;;) {
+		long lvl = (long)((w + 3) / 4) * ((h + 3) / 4) * bs;
+		uint8_t *t;
+		s2tc_oracle_compress_ex(4, w, h, pic, fmt, o, ((w + 3) / 4) * (int)bs, dither, metric, nrandom, refine,
+					&prev_a1);
+		o += lvl;
+		if (w == 1 && h == 1) break;
+		s2tc_oracle_mip_reduce(pic, next, &w, &h);
+		t = pic; pic = next; next = t;
+	}
+	free(pic);
+	free(next);
+	return (long)(o - out);
+}
+
+/* s2tc_decompress (s2tc_decompress.c:156-207): the base level of a DXT1/3/5
+ * DDS (height and width from header words 3 and 4, FourCC from word 21; DXT1
+ * decodes with the RGBA variant) as an 18-byte TGA header and top-down BGRA
+ * rows.  Returns the bytes written, or -1 for another FourCC. */
+long s2tc_oracle_decompress(const uint8_t *dds, uint8_t *tga)
+{
+	int height = (int)get32(dds + 12), width = (int)get32(dds + 16), x, y, dxt;
+	uint32_t fourcc = get32(dds + 84);
+	uint8_t *o = tga + 18;
+	if (fourcc == 0x31545844) dxt = S2TC_O_DXT1;
+	else if (fourcc == 0x33545844) dxt = S2TC_O_DXT3;
+	else if (fourcc == 0x35545844) dxt = S2TC_O_DXT5;
+	else return -1;
+	memset(tga, 0, 18);
+	tga[2] = 2;
+	tga[12] = (uint8_t)(width % 256);
+	tga[13] = (uint8_t)(width / 256);
+	tga[14] = (uint8_t)(height % 256);
+	tga[15] = (uint8_t)(height / 256);
+	tga[16] = 32;
+	tga[17] = 0x28;
+	for (y = 0; y < height; ++y)
+		for (x = 0; x < width; ++x) {
+			uint8_t t[4];
+			s2tc_oracle_fetch(dxt, 1, width, dds + 128, x, y, t);
+			o[0] = t[2]; o[1] = t[1]; o[2] = t[0]; o[3] = t[3];
+			o += 4;
+		}
+	return (long)(o - tga);
+}
+
+/* s2tc_from_s3tc's colour block rewrite (s2tc_from_s3tc.cpp:77-143): every
+ * index becomes 0 or 1 (index 2 and 3 map to the endpoint chosen by the
+ * reference's bit formula), then the endpoints are put in S2TC order (c0 < c1
+ * for a DXT1 block that keeps its transparent texels, else c0 > c1), with the
+ * indices inverted on a swap.  `alpha` selects the DXT1 variant that keeps
+ * index 3 as transparent when c1 >= c0. */
+static void from_s3tc_colour(uint8_t *b, int alpha)
+{
+	unsigned c = b[0] | (b[1] << 8), c1 = b[2] | (b[3] << 8), t;
+	uint32_t px = get32(b + 4);
+	int swap;
+	if (c1 >= c) {
+		if (alpha) px = (px & ~((~px & 0x55555555u) << 1)) | ((px & 0x22882288u) >> 1);
+		else px = (px & ((~px & 0xAAAAAAAAu) >> 1)) | ((px & 0x22882288u) >> 1);
+		swap = !alpha;
+	} else {
+		px = (px & ((~px & 0xAAAAAAAAu) >> 1)) | ((px & 0x22882288u) >> 1);
+		swap = alpha;
+	}
+	if (swap) {
+		t = c; c = c1; c1 = t;
+		px ^= 0x55555555u;
+	}
+	b[0] = (uint8_t)c; b[1] = (uint8_t)(c >> 8); b[2] = (uint8_t)c1; b[3] = (uint8_t)(c1 >> 8);
+	put32(b + 4, px);
+}
+
+/* DXT5 alpha block rewrite (s2tc_from_s3tc.cpp:145-190): 3-bit indices 2..5
+ * (and 6, 7 when a1 < a0) become 0 or 1, then a0 <= a1 order with the 0/1
+ * indices inverted on a swap. */
+static void from_s3tc_alpha(uint8_t *b)
+{
+	unsigned a = b[0], a1 = b[1], t;
+	uint64_t px = 0, sel;
+	const uint64_t ones = 01111111111111111ull, pick = 00101101001011010ull;
+	int k;
+	for (k = 0; k < 6; ++k) px |= (uint64_t)b[2 + k] << (8 * k);
+	if (a1 >= a) {
+		sel = (px >> 1) ^ (px >> 2);
+		px = (px & ~((sel & ones) * 7)) | (sel & pick);
+	} else {
+		sel = (px >> 1) | (px >> 2);
+		px = (px & ~((sel & ones) * 7)) | (sel & pick);
+		t = a; a = a1; a1 = t;
+		px ^= ones;
+	}
+	b[0] = (uint8_t)a;
+	b[1] = (uint8_t)a1;
+	for (k = 0; k < 6; ++k) b[2 + k] = (uint8_t)(px >> (8 * k));
+}
+
+/* One block of format `dxt` (s2tc_from_s3tc.cpp:255-262). */
+void s2tc_oracle_from_s3tc_block(int dxt, uint8_t *blk)
+{
+	if (dxt == S2TC_O_DXT1) {
+		from_s3tc_colour(blk, 1);
+	} else {
+		from_s3tc_colour(blk + 8, 0);
+		if (dxt == S2TC_O_DXT5) from_s3tc_alpha(blk);
+	}
+}
+
+/* s2tc_from_s3tc on a whole file (s2tc_from_s3tc.cpp:209-269): the 128-byte
+ * header is copied, then every whole block that follows is converted (a
+ * trailing partial block is dropped, as the reference's fread loop does).
+ * Returns the bytes written, or -1 for another FourCC or a file shorter than
+ * the header. */
+long s2tc_oracle_from_s3tc(const uint8_t *in, long size, uint8_t *out)
+{
+	uint32_t fourcc;
+	int dxt;
+	long bs, n, i;
+	if (size < 128) return -1;
+	fourcc = get32(in + 84);
+	if (fourcc == 0x31545844) dxt = S2TC_O_DXT1;
+	else if (fourcc == 0x33545844) dxt = S2TC_O_DXT3;
+	else if (fourcc == 0x35545844) dxt = S2TC_O_DXT5;
+	else return -1;
+	bs = dxt == S2TC_O_DXT1 ? 8 : 16;
+	n = (size - 128) / bs;
+	memcpy(out, in, 128);
+	memcpy(out + 128, in + 128, (size_t)(n * bs));
+	for (i = 0; i < n; ++i) s2tc_oracle_from_s3tc_block(dxt, out + 128 + i * bs);
+	return 128 + n * bs;
 }

@@ -33,6 +33,14 @@ int s2tc_oracle_compress(int srccomps, int width, int height, const uint8_t *src
 			 int dither, int metric, int nrandom, int refine);
 void s2tc_oracle_fetch(int dxt, int rgba_dxt1, int stride, const uint8_t *data, int i, int j,
 		       uint8_t *texel);
+/* the reference's command-line tools, in memory */
+void s2tc_oracle_mip_reduce(const uint8_t *in, uint8_t *out, int *width, int *height);
+long s2tc_oracle_dds_size(int width, int height, unsigned int fmt);
+long s2tc_oracle_dds(const uint8_t *rgba, int width, int height, unsigned int fmt,
+		     int dither, int metric, int nrandom, int refine, uint8_t *out);
+long s2tc_oracle_decompress(const uint8_t *dds, uint8_t *tga);
+void s2tc_oracle_from_s3tc_block(int dxt, uint8_t *blk);
+long s2tc_oracle_from_s3tc(const uint8_t *in, long size, uint8_t *out);
 
 #ifdef __cplusplus
 }

@@ -137,6 +137,19 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_server_stats.restype = c_int
     lib.s2tc_server_destroy.argtypes = [vp]
     lib.s2tc_server_destroy.restype = None
+    lib.s2tc_dds_size.argtypes = [c_int, c_int, c_uint]
+    lib.s2tc_dds_size.restype = c_ll
+    lib.s2tc_compress_dds.argtypes = [vp, c_int, c_int, c_uint, ctypes.POINTER(Options), vp, c_ll,
+                                      ctypes.POINTER(c_ll)]
+    lib.s2tc_compress_dds.restype = c_int
+    lib.s2tc_gpu_decode.argtypes = [vp, c_uint, c_int, c_int, vp, c_ll, c_int, vp]
+    lib.s2tc_gpu_decode.restype = c_int
+    lib.s2tc_decompress_dds.argtypes = [vp, c_ll, vp, c_ll, ctypes.POINTER(c_ll)]
+    lib.s2tc_decompress_dds.restype = c_int
+    lib.s2tc_gpu_from_s3tc.argtypes = [vp, vp, c_ll, c_uint, vp]
+    lib.s2tc_gpu_from_s3tc.restype = c_int
+    lib.s2tc_from_s3tc_dds.argtypes = [vp, c_ll, vp, c_ll, ctypes.POINTER(c_ll)]
+    lib.s2tc_from_s3tc_dds.restype = c_int
     lib.s2tc_last_error.argtypes = []
     lib.s2tc_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -153,6 +166,8 @@ EXPORTED_SYMBOLS = (
     "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
     "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit",
     "s2tc_server_wait", "s2tc_server_stats", "s2tc_server_destroy",
+    "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
+    "s2tc_gpu_from_s3tc", "s2tc_from_s3tc_dds",
     "s2tc_last_error",
 )
 
@@ -411,6 +426,65 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------- the reference's tools
+
+def dds_size(width: int, height: int, fmt: int) -> int:
+    return int(load().s2tc_dds_size(width, height, fmt))
+
+
+def compress_dds(rgba, width: int, height: int, fmt: int, opt: Options | None = None) -> bytes:
+    """``s2tc_compress_dds``: the DDS file s2tc_compress writes for an RGBA8
+    image (every mip level to 1x1).  ``opt`` None reads the S2TC_* env."""
+    src = np.ascontiguousarray(rgba, dtype=np.uint8).reshape(-1)
+    n = dds_size(width, height, fmt)
+    if n < 0:
+        raise S2tcError("bad format or size")
+    out = np.zeros(n, np.uint8)
+    written = ctypes.c_longlong()
+    st = load().s2tc_compress_dds(_ptr(src), width, height, fmt, ctypes.byref(opt) if opt is not None else None,
+                                  _ptr(out), n, ctypes.byref(written))
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_compress_dds failed ({st}): {last_error()}")
+    return out[: written.value].tobytes()
+
+
+def gpu_decode(d_blocks, fmt: int, width: int, height: int, d_out, dst_pitch: int = 0, bgra: bool = False,
+               stream: int | None = None) -> None:
+    st = load().s2tc_gpu_decode(_addr(d_blocks), fmt, width, height, _addr(d_out), dst_pitch, int(bgra), stream)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_decode failed ({st})")
+
+
+def decompress_dds(dds: bytes) -> bytes:
+    """``s2tc_decompress_dds``: the TGA s2tc_decompress writes."""
+    src = np.frombuffer(dds, np.uint8).copy()
+    w = int.from_bytes(dds[16:20], "little") if len(dds) >= 20 else 0
+    h = int.from_bytes(dds[12:16], "little") if len(dds) >= 16 else 0
+    out = np.zeros(18 + 4 * max(0, w) * max(0, h), np.uint8)
+    written = ctypes.c_longlong()
+    st = load().s2tc_decompress_dds(_ptr(src), src.size, _ptr(out), out.size, ctypes.byref(written))
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_decompress_dds failed ({st})")
+    return out[: written.value].tobytes()
+
+
+def gpu_from_s3tc(d_src, d_dst, nblocks: int, fmt: int, stream: int | None = None) -> None:
+    st = load().s2tc_gpu_from_s3tc(_addr(d_src), _addr(d_dst), nblocks, fmt, stream)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_from_s3tc failed ({st})")
+
+
+def from_s3tc_dds(dds: bytes) -> bytes:
+    """``s2tc_from_s3tc_dds``: the file s2tc_from_s3tc writes."""
+    src = np.frombuffer(dds, np.uint8).copy()
+    out = np.zeros(max(128, src.size), np.uint8)
+    written = ctypes.c_longlong()
+    st = load().s2tc_from_s3tc_dds(_ptr(src), src.size, _ptr(out), out.size, ctypes.byref(written))
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_from_s3tc_dds failed ({st})")
+    return out[: written.value].tobytes()
 
 
 def _addr(x) -> int:

@@ -21,6 +21,7 @@
 
 #include "dither.h"
 #include "encode.h"
+#include "tools.h"
 #include "s2tc_types.h"
 
 namespace s2tc {
@@ -86,6 +87,7 @@ struct Context {
   std::vector<cudaEvent_t> ev;   // 3 per slot: before dither, between, after encode
   long long timed_calls = 0;
   DevBuf src, t565, dst, scratch, rnd, err;
+  DevBuf mips, blocks;  // s2tc_compress_dds: every level's pixels and blocks
   PinnedBuf host_rnd, host_out;
 
   bool init() {
@@ -100,6 +102,8 @@ struct Context {
     if (!cuda_ok(cudaEventCreateWithFlags(&arena_free, cudaEventDisableTiming), "cudaEventCreate")) return false;
     if (!err.reserve(sizeof(int) * 4, "cudaMalloc(error flag)")) return false;
     if (!cuda_ok(cudaMemset(err.p, 0, sizeof(int) * 4), "cudaMemset")) return false;
+    // err[2]: the carried alpha endpoint of tx_compress_dxtn calls (-1: none yet)
+    if (!cuda_ok(cudaMemset(err.as<int>() + 2, 0xFF, sizeof(int)), "cudaMemset")) return false;
     ready = true;
     return true;
   }
@@ -174,9 +178,16 @@ int rand_per_block(const s2tc_options& o, int dxt) {
 // order, into pinned memory, then to the device.
 constexpr long long kRandChunkWords = 1ll << 24;
 
+// `carry` (device int, may be null): the second alpha endpoint that the
+// previous call's last block left behind.  The reference encodes every block
+// of every call in the same stack frame, and a DXT5 image whose first block
+// has a single texel (a 1x1 image, e.g. the last level of a mip chain) reads
+// its second alpha candidate from that frame without writing it first
+// (s2tc_algorithm.cpp:996-1001), i.e. it sees the previous call's leftover.
+// All-texel DXT5 calls read and update it; other calls leave it alone.
 int compress_device_locked(Context& c, int srccomps, int width, int height, const uint8_t* d_src, int dxt,
                            uint8_t* d_dst, long long pitch, const s2tc_options& opt, const unsigned int* d_rand,
-                           cudaStream_t s) {
+                           cudaStream_t s, int* carry = nullptr) {
   const int sc = srccomps == 3 ? 3 : 4;
   const long long npx = (long long)width * height;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4;
@@ -212,9 +223,14 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
   ea.aligned = ((reinterpret_cast<uintptr_t>(d_dst) % bs) == 0 && (pitch % bs) == 0) ? 1 : 0;
   ea.nrandom = opt.nrandom;
   ea.prev_a1_first = -1;
+  ea.prev_a1_dev = nullptr;
   ea.leftover_out = nullptr;
   const bool normal = normal_mode(opt);
   const int per_block = rand_per_block(opt, dxt);
+  if (carry && dxt == DXT5 && normal && per_block == 0) {
+    ea.prev_a1_dev = carry;
+    ea.leftover_out = carry;
+  }
   if (per_block == 0) {
     ea.by0 = 0;
     ea.nby = bh;
@@ -286,7 +302,7 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
   if (!c.dst.reserve(row_bytes * bh + 16, "cudaMalloc(dst)")) return;
   if (!cuda_ok(cudaMemcpyAsync(c.src.p, src, in_bytes, cudaMemcpyHostToDevice, s), "input upload")) return;
   if (compress_device_locked(c, sc, width, height, c.src.as<uint8_t>(), dxt, c.dst.as<uint8_t>(), (long long)row_bytes,
-                             opt, nullptr, s) != ST_OK)
+                             opt, nullptr, s, c.err.as<int>() + 2) != ST_OK)
     return;
   if (check_error_flag(c, s) != ST_OK) return;
   // Output rows: packed, or dstRowStride apart (s2tc_libtxc_dxtn.cpp:243, 261, 279).
@@ -965,6 +981,114 @@ void s2tc_batch_destroy(s2tc_batch* h) {
 }
 
 int s2tc_batch_kernels(const s2tc_batch* h) { return h ? h->impl.kernels : 0; }
+
+long long s2tc_dds_size(int width, int height, unsigned int format) {
+  const int dxt = format_dxt(format);
+  if (dxt < 0 || width <= 0 || height <= 0) return -1;
+  const long long bs = s2tc::block_bytes(dxt);
+  long long n = 128;
+  int w = width, h = height;
+  for (;;) {
+    n += (long long)((w + 3) / 4) * ((h + 3) / 4) * bs;
+    if (w == 1 && h == 1) break;
+    s2tc::mip_next(w, h);
+  }
+  return n;
+}
+
+// s2tc_compress (s2tc_compress.c:594-719) from its RGBA buffer on: the DDS
+// header, then every mip level from the base to 1x1.  The levels are built on
+// the device (one mip kernel per level), then each is compressed exactly as a
+// tx_compress_dxtn call would (same kernels, libc rand() replayed per level in
+// order, the leftover alpha endpoint carried from level to level), on one
+// stream with a single synchronisation at the end.
+int s2tc_compress_dds(const void* rgba, int width, int height, unsigned int format, const s2tc_options* opt, void* out,
+                      long long out_size, long long* written) {
+  using namespace s2tc;
+  if (written) *written = 0;
+  const int dxt = format_dxt(format);
+  if (dxt < 0) {
+    set_error("bad destination format");
+    return S2TC_ERR_FORMAT;
+  }
+  if (!rgba || !out || width <= 0 || height <= 0 || width > 32768 || height > 32768) {
+    set_error("bad argument");
+    return S2TC_ERR_ARGUMENT;
+  }
+  const long long total = s2tc_dds_size(width, height, format);
+  if (out_size < total) {
+    set_error("output buffer smaller than s2tc_dds_size");
+    return S2TC_ERR_ARGUMENT;
+  }
+  const s2tc_options o = normalise(opt ? *opt : read_env());
+  const long long bs = block_bytes(dxt);
+  // level sizes and offsets
+  struct Level {
+    int w, h;
+    long long px_off, blk_off;
+  };
+  std::vector<Level> levels;
+  long long px_total = 0, blk_total = 0;
+  for (int w = width, h = height;;) {
+    levels.push_back(Level{w, h, px_total, blk_total});
+    px_total += ((long long)w * h * 4 + 15) & ~15ll;
+    blk_total += (long long)((w + 3) / 4) * ((h + 3) / 4) * bs;
+    if (w == 1 && h == 1) break;
+    mip_next(w, h);
+  }
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  cudaStream_t s = c.stream;
+  if (!c.mips.reserve(size_t(px_total) + 16, "cudaMalloc(mip levels)")) return S2TC_ERR_NOMEM;
+  if (!c.blocks.reserve(size_t(blk_total) + 16, "cudaMalloc(blocks)")) return S2TC_ERR_NOMEM;
+  uint8_t* px = c.mips.as<uint8_t>();
+  uint8_t* blk = c.blocks.as<uint8_t>();
+  int* alpha_flag = c.err.as<int>() + 3;
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return S2TC_ERR_CUDA;
+  if (!cuda_ok(cudaMemcpyAsync(px, rgba, size_t(width) * height * 4, cudaMemcpyHostToDevice, s), "input upload"))
+    return S2TC_ERR_CUDA;
+  if (!cuda_ok(cudaMemsetAsync(alpha_flag, 0, sizeof(int), s), "cudaMemsetAsync")) return S2TC_ERR_CUDA;
+  if (!cuda_ok(launch_any_alpha(px, (long long)width * height, alpha_flag, s), "alpha test")) return S2TC_ERR_CUDA;
+  for (size_t l = 1; l < levels.size(); ++l)
+    if (!cuda_ok(launch_mip_reduce(px + levels[l - 1].px_off, levels[l - 1].w, levels[l - 1].h, px + levels[l].px_off,
+                                   s),
+                 "mip reduce"))
+      return S2TC_ERR_CUDA;
+  for (const Level& L : levels) {
+    const int st = compress_device_locked(c, 4, L.w, L.h, px + L.px_off, dxt, blk + L.blk_off,
+                                          (long long)((L.w + 3) / 4) * bs, o, nullptr, s, c.err.as<int>() + 2);
+    if (st != ST_OK) return st;
+  }
+  unsigned char* o8 = static_cast<unsigned char*>(out);
+  int alpha = 0;
+  if (!cuda_ok(cudaMemcpyAsync(o8 + 128, blk, size_t(blk_total), cudaMemcpyDeviceToHost, s), "output download"))
+    return S2TC_ERR_CUDA;
+  if (!cuda_ok(cudaMemcpyAsync(&alpha, alpha_flag, sizeof(int), cudaMemcpyDeviceToHost, s), "flag download"))
+    return S2TC_ERR_CUDA;
+  const int st = check_error_flag(c, s);
+  if (st != ST_OK) return st;
+  // the header (s2tc_compress.c:662-707)
+  auto put = [&](int off, uint32_t v) {
+    for (int i = 0; i < 4; ++i) o8[off + i] = uint8_t(v >> (8 * i));
+  };
+  int mipcount = 0;
+  while (width >= (1 << mipcount) || height >= (1 << mipcount)) ++mipcount;
+  std::memset(o8, 0, 128);
+  std::memcpy(o8, "DDS ", 4);
+  put(4, 0x7c);
+  put(8, 0x000a1007);
+  put(12, uint32_t(height));
+  put(16, uint32_t(width));
+  put(20, uint32_t(((width + 3) / 4) * ((height + 3) / 4) * bs));
+  put(28, uint32_t(mipcount));
+  put(76, 0x20);
+  put(80, alpha ? 5 : 4);
+  std::memcpy(o8 + 84, dxt == s2tc::DXT1 ? "DXT1" : dxt == s2tc::DXT3 ? "DXT3" : "DXT5", 4);
+  put(108, 0x00401008);
+  if (written) *written = total;
+  return S2TC_OK;
+}
 
 const char* s2tc_last_error(void) { return s2tc::g_last_error.c_str(); }
 

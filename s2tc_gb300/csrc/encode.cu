@@ -449,7 +449,8 @@ __global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encod
   load_block(a.t565, a.width, a.height, bx, by, bt);
   if (!is_full<DXT>(bt)) return;  // left to k_encode
   EncodedBlock eb;
-  encode_block<DXT, true, REFINE, true>(bt, 0, nullptr, -1, eb, sc);
+  const int leftover = encode_block<DXT, true, REFINE, true>(bt, 0, nullptr, -1, eb, sc);
+  if (a.leftover_out && b == (long long)a.bw * a.bh - 1) *a.leftover_out = leftover;
   store_block(a, DXT, bx, by, eb);
 }
 
@@ -483,7 +484,7 @@ __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
       EncodedBlock scratch;
       prev_a1 = encode_block<DXT, NORMAL, REFINE, false>(pt, a.nrandom, nullptr, -1, scratch, sc);
     } else {
-      prev_a1 = a.prev_a1_first;
+      prev_a1 = a.prev_a1_dev ? *a.prev_a1_dev : a.prev_a1_first;
     }
   }
   EncodedBlock eb;

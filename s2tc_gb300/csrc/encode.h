@@ -19,6 +19,8 @@ struct EncodeArgs {
                          // order, starting at block row by0
   int prev_a1_first;     // second alpha endpoint left by the block before block 0
                          // (-1: none); see encode.cu
+  const int* prev_a1_dev;  // if set, that value is read from device memory instead
+                           // (it may be this launch's own leftover_out)
   int* leftover_out;     // if set, receives the last block's leftover alpha endpoint
 };
 
