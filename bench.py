@@ -64,6 +64,13 @@ WORKLOADS = {
     "normal_maps_64x2048_dxt1_normalmap_rand64_loop": dict(
         w=2048, h=2048, sc=3, fmt=0x83F1, dither=1, metric=7, nrandom=64, refine=2, gen="normal_batch", seed=4,
         count=64, distinct=16),
+    # the reference's tools on the GPU: whole-image decode (s2tc_decompress),
+    # S3TC -> S2TC block rewrite (s2tc_from_s3tc), mip chain + DDS
+    # (s2tc_compress); HBM-bound except the DDS pipeline's encoder
+    "decode_8192_dxt5": dict(w=8192, h=8192, sc=4, fmt=0x83F3, gen="tool", tool="decode", seed=6),
+    "from_s3tc_8192_dxt5": dict(w=8192, h=8192, sc=4, fmt=0x83F3, gen="tool", tool="from_s3tc", seed=7),
+    "dds_4096_dxt1_wavg_quick_always": dict(w=4096, h=4096, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1,
+                                            gen="tool", tool="dds", seed=1),
     # requests of log-uniform size 64..4096, DXT1/DXT5, WAVG/SRGB_MIXED/NORMALMAP,
     # through the continuous-batching request loop under a 32 GB budget; a
     # step is 1000 requests
@@ -97,6 +104,16 @@ def algorithmic_bytes_per_texel(wl: dict) -> float:
 
 def config_dict(wl_name: str, wl: dict) -> dict:
     import s2tc_gb300 as s2
+    if wl["gen"] == "tool":
+        d = {"workload": wl_name, "width": wl["w"], "height": wl["h"], "format": FMT_NAMES[wl["fmt"]],
+             "tool": {"decode": "s2tc_decompress (s2tc_gpu_decode)", "from_s3tc": "s2tc_from_s3tc (s2tc_gpu_from_s3tc)",
+                      "dds": "s2tc_compress (s2tc_compress_dds, every mip level)"}[wl["tool"]],
+             "l2": "inputs and outputs larger than the 129 MB L2"}
+        if wl["tool"] == "dds":
+            d.update(dither=s2.DITHER_NAMES[wl["dither"]], colordist=s2.COLORDIST_NAMES[wl["metric"]],
+                     random_colors=wl["nrandom"], refine=s2.REFINE_NAMES[wl["refine"]],
+                     l2="one 64 MB image and its levels; timed end to end per call")
+        return d
     if wl["gen"] == "normal_batch":
         return {"workload": wl_name, "maps": wl["count"], "distinct_maps": wl["distinct"], "width": wl["w"],
                 "height": wl["h"], "srccomps": 3, "format": "DXT1", "dither": s2.DITHER_NAMES[wl["dither"]],
@@ -417,6 +434,149 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------- tool workloads
+
+def run_tool_workload(args, wl_name: str, wl: dict) -> None:
+    """The reference's tools on the GPU.  decode / from_s3tc: device-resident
+    blocks (two rotating inputs larger than L2), CUDA events around K launches;
+    e2e through the in-memory file entry points.  dds: s2tc_compress_dds with
+    host buffers (it is end to end by construction)."""
+    import torch
+    import s2tc_gb300 as s2
+    from s2tc_gb300 import workloads
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    w, h, fmt = wl["w"], wl["h"], wl["fmt"]
+    npx = w * h
+    bs = 8 if fmt in (0x83F0, 0x83F1) else 16
+    nblocks = ((w + 3) // 4) * ((h + 3) // 4)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    oracle = pyoracle.Oracle()
+    rng = np.random.default_rng(wl["seed"])
+    cpu = None
+    if wl["tool"] in ("decode", "from_s3tc"):
+        blocks = [rng.integers(0, 256, nblocks * bs, dtype=np.uint8) for _ in range(2)]
+        d_in = [torch.from_numpy(b).cuda() for b in blocks]
+        if wl["tool"] == "decode":
+            d_out = [torch.empty(npx * 4, dtype=torch.uint8, device="cuda") for _ in range(2)]
+            launch = lambda i: s2.gpu_decode(d_in[i % 2], fmt, w, h, d_out[i % 2], 0, False, sp)
+            alg = nblocks * bs + npx * 4
+        else:
+            d_out = [torch.empty_like(x) for x in d_in]
+            launch = lambda i: s2.gpu_from_s3tc(d_in[i % 2], d_out[i % 2], nblocks, fmt, sp)
+            alg = 2 * nblocks * bs
+        for i in range(args.warmup):
+            launch(i)
+        torch.cuda.synchronize()
+        l0 = s2.kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(stream)
+            for i in range(args.steps):
+                launch(i)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        launches = s2.kernel_launches() - l0
+        t = e0.elapsed_time(e1) / 1000.0
+        value = args.steps * npx / t
+        achieved = alg / (t / args.steps) / 1e9
+        # parity of the timed kernel on a sample of its output
+        if wl["tool"] == "decode":
+            got = d_out[0].cpu().numpy().reshape(h, w, 4)
+            for (i, j) in ((0, 0), (w - 1, h - 1), (1234, 567), (w // 2, h // 3)):
+                assert np.array_equal(got[j, i], oracle.fetch(2 if fmt == 0x83F3 else 0, 1, w, blocks[0], i, j))
+        else:
+            got = d_out[0][: 1000 * bs].cpu().numpy()
+            assert np.array_equal(got, oracle.from_s3tc_blocks(blocks[0][: 1000 * bs], 2 if fmt == 0x83F3 else 0))
+        # end to end through the in-memory file entry point
+        hdr = bytearray(128)
+        hdr[0:4] = b"DDS "
+        hdr[12:16] = h.to_bytes(4, "little")
+        hdr[16:20] = w.to_bytes(4, "little")
+        hdr[84:88] = (b"DXT5" if fmt == 0x83F3 else b"DXT1")
+        dds = bytes(hdr) + blocks[0].tobytes()
+        fn = s2.decompress_dds if wl["tool"] == "decode" else s2.from_s3tc_dds
+        fn(dds)
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 4)):
+            fn(dds)
+        t_e2e = (time.perf_counter() - t0) / max(1, args.steps // 4)
+        e2e = {"value": npx / t_e2e, "unit": "texels/s", "h2d_bytes_per_step": len(dds),
+               "d2h_bytes_per_step": (18 + npx * 4) if wl["tool"] == "decode" else len(dds),
+               "ms_per_step": 1000 * t_e2e, "note": "host file in, host file out, pageable buffers"}
+        if not args.no_cpu_baseline:
+            rows = 512
+            if wl["tool"] == "decode":
+                sub = bytes(hdr[:12]) + rows.to_bytes(4, "little") + bytes(hdr[16:]) + \
+                    blocks[0][: (rows // 4) * (w // 4) * bs].tobytes()
+                c0 = time.perf_counter()
+                oracle.decompress(sub)
+            else:
+                sub = bytes(hdr) + blocks[0][: (rows // 4) * (w // 4) * bs].tobytes()
+                c0 = time.perf_counter()
+                oracle.from_s3tc(sub)
+            dt = time.perf_counter() - c0
+            cpu = {"value": rows * w / dt, "unit": "texels/s", "cores": 1, "kind": "port",
+                   "sample": f"the first {rows} rows ({rows * w} texels), single thread ({dt:.2f} s)"}
+        kernel = "k_decode" if wl["tool"] == "decode" else "k_from_s3tc"
+        roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                    "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_launch": alg}
+        ms = 1000 * t / args.steps
+    else:
+        img = workloads.plain_rgba(wl["seed"], w, h)
+        opt = s2.options(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+        out0 = s2.compress_dds(img, w, h, fmt, opt)
+        for _ in range(args.warmup - 1):
+            s2.compress_dds(img, w, h, fmt, opt)
+        l0 = s2.kernel_launches()
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                s2.compress_dds(img, w, h, fmt, opt)
+            t = time.perf_counter() - t0
+        launches = s2.kernel_launches() - l0
+        levels_tex = 0
+        lw, lh = w, h
+        while True:
+            levels_tex += lw * lh
+            if lw == 1 and lh == 1:
+                break
+            lw, lh = max(1, lw // 2), max(1, lh // 2)
+        value = args.steps * levels_tex / t
+        ms = 1000 * t / args.steps
+        e2e = {"value": value, "unit": "texels/s", "h2d_bytes_per_step": npx * 4, "d2h_bytes_per_step": len(out0),
+               "ms_per_step": ms, "note": "host RGBA in, host DDS file out; the call is the step"}
+        alg = levels_tex * 4 + len(out0)
+        achieved = alg / (t / args.steps) / 1e9
+        roofline = {"bound": "hbm", "kernel": "pipeline", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                    "frac": achieved / hbm, "traffic": None,
+                    "note": "whole call including host copies; the encoder is integer-bound"}
+        if not args.no_cpu_baseline:
+            small = np.ascontiguousarray(img[:512, :512])
+            c0 = time.perf_counter()
+            want = oracle.dds(small, 512, 512, fmt, wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+            dt = time.perf_counter() - c0
+            got = s2.compress_dds(small, 512, 512, fmt, opt)
+            cpu = {"value": (512 * 512 * 4 // 3) / dt, "unit": "texels/s", "cores": 1, "kind": "port",
+                   "sample": f"a 512x512 crop with its mip chain, single thread ({dt:.2f} s)",
+                   "bit_exact": got == want}
+    line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": config_dict(wl_name, wl),
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------- serving workload
 
 def _lindley(arrivals, service):
@@ -609,7 +769,7 @@ def main() -> None:
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
-        if wl["gen"] in ("mips", "serving", "normal_batch"):
+        if wl["gen"] in ("mips", "serving", "normal_batch", "tool"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times single-image workloads"}))
             return
         run_reference_arm(args, args.workload, wl)
@@ -619,6 +779,9 @@ def main() -> None:
         return
     if wl["gen"] == "serving":
         run_serving_workload(args, args.workload, wl)
+        return
+    if wl["gen"] == "tool":
+        run_tool_workload(args, args.workload, wl)
         return
 
     import torch

@@ -112,50 +112,56 @@ __global__ void k_decode(const uint8_t* __restrict__ blocks, int rgba_dxt1, int 
   const uint64_t alpha = DXT == DXT1 ? 0 : load8(blk);
   const uint32_t c = uint32_t(colour) & 0xFFFFu, c1 = uint32_t(colour >> 16) & 0xFFFFu;
   const uint32_t idx = uint32_t(colour >> 32);
-  const uint32_t col0 = expand565(c), col1 = expand565(c1);
-  const uint32_t a0 = uint32_t(alpha) & 0xFFu, a1 = uint32_t(alpha >> 8) & 0xFFu;
-  const int cw = min(4, width - 4 * bx), ch = min(4, height - 4 * by);
-#pragma unroll
-  for (int y = 0; y < 4; ++y) {
-    if (y >= ch) break;
-    uint32_t row[4];
-#pragma unroll
-    for (int x = 0; x < 4; ++x) {
-      const bool odd = ((x ^ y) & 1) != 0;
-      const uint32_t sel = (idx >> (8 * y + 2 * x)) & 3u;
-      uint32_t rgb, a = 255;
-      if (sel == 0) rgb = col0;
-      else if (sel == 1) rgb = col1;
-      else if (DXT == DXT1 && sel == 3 && c1 >= c) {
-        rgb = 0;
-        if (rgba_dxt1) a = 0;
-      } else {
-        rgb = odd ? col1 : col0;
-      }
-      if (DXT == DXT3) {
-        const uint32_t a4 = uint32_t(alpha >> (16 * y + 4 * x)) & 15u;
-        a = a4 | (a4 << 4);
-      } else if (DXT == DXT5) {
-        const uint32_t ab = uint32_t(alpha >> (16 + 3 * (4 * y + x))) & 7u;
-        if (ab == 1) a = a1;
-        else if (ab == 6 && a1 >= a0) a = 0;
-        else if (ab == 7 && a1 >= a0) a = 255;
-        else if (ab >= 2 && odd) a = a1;
-        else a = a0;
-      }
-      if (bgra) rgb = __byte_perm(rgb, 0, 0x3012);
-      row[x] = rgb | (a << 24);
-    }
-    uint8_t* o = out + (long long)(4 * by + y) * pitch + (long long)(4 * bx) * 4;
-    if (cw == 4 && (reinterpret_cast<uintptr_t>(o) & 15) == 0) {
-      *reinterpret_cast<uint4*>(o) = make_uint4(row[0], row[1], row[2], row[3]);
-    } else if ((reinterpret_cast<uintptr_t>(o) & 3) == 0) {
-      for (int x = 0; x < cw; ++x) reinterpret_cast<uint32_t*>(o)[x] = row[x];
-    } else {
-      for (int x = 0; x < cw; ++x)
-        for (int b = 0; b < 4; ++b) o[4 * x + b] = uint8_t(row[x] >> (8 * b));
-    }
+  uint32_t col0 = expand565(c), col1 = expand565(c1);
+  if (bgra) {
+    col0 = __byte_perm(col0, 0, 0x3012);
+    col1 = __byte_perm(col1, 0, 0x3012);
   }
+  const uint32_t a0 = uint32_t(alpha) & 0xFFu, a1 = uint32_t(alpha >> 8) & 0xFFu;
+  const bool trans_ok = DXT == DXT1 && c1 >= c;  // index 3 is transparent black
+  const uint32_t trans_a = rgba_dxt1 ? 0u : 255u;
+  // all 16 texels without branches (slot s = 4y + x; index bits 2s)
+  uint32_t t[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    const int x = s & 3, y = s >> 2;
+    const bool odd = ((x ^ y) & 1) != 0;
+    const uint32_t sel = (idx >> (2 * s)) & 3u;
+    const bool one = sel == 1 || (sel >= 2 && odd);
+    const bool trans = trans_ok && sel == 3;
+    uint32_t rgb = one ? col1 : col0;
+    rgb = trans ? 0u : rgb;
+    uint32_t a = trans ? trans_a : 255u;
+    if (DXT == DXT3) {
+      const uint32_t a4 = uint32_t(alpha >> (4 * s)) & 15u;
+      a = a4 | (a4 << 4);
+    } else if (DXT == DXT5) {
+      const uint32_t ab = uint32_t(alpha >> (16 + 3 * s)) & 7u;
+      const bool hi = a1 >= a0;
+      a = (ab >= 2 && odd) ? a1 : a0;
+      a = (ab == 7 && hi) ? 255u : a;
+      a = (ab == 6 && hi) ? 0u : a;
+      a = ab == 1 ? a1 : a;
+    }
+    t[s] = rgb | (a << 24);
+  }
+  const int cw = min(4, width - 4 * bx), ch = min(4, height - 4 * by);
+  uint8_t* o = out + (long long)(4 * by) * pitch + (long long)(4 * bx) * 4;
+  if (cw == 4 && ch == 4 && ((reinterpret_cast<uintptr_t>(o) | uintptr_t(pitch)) & 15) == 0) {
+#pragma unroll
+    for (int y = 0; y < 4; ++y)
+      *reinterpret_cast<uint4*>(o + y * pitch) = make_uint4(t[4 * y], t[4 * y + 1], t[4 * y + 2], t[4 * y + 3]);
+    return;
+  }
+  for (int y = 0; y < ch; ++y)
+    for (int x = 0; x < cw; ++x) {
+      uint8_t* q = o + y * pitch + 4 * x;
+      if ((reinterpret_cast<uintptr_t>(q) & 3) == 0) {
+        *reinterpret_cast<uint32_t*>(q) = t[4 * y + x];
+      } else {
+        for (int b = 0; b < 4; ++b) q[b] = uint8_t(t[4 * y + x] >> (8 * b));
+      }
+    }
 }
 
 // --------------------------------------------------------------- from_s3tc
@@ -211,6 +217,10 @@ __global__ void k_from_s3tc(const uint8_t* src, uint8_t* dst, long long nblocks)
     uint8_t* d = dst + k * bs;
     if (DXT == DXT1) {
       store8(d, s3tc_colour(load8(s), true));
+    } else if (((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d)) & 15) == 0) {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(s);  // src may be dst
+      *reinterpret_cast<ulonglong2*>(d) =
+          make_ulonglong2(DXT == DXT5 ? s3tc_alpha(v.x) : v.x, s3tc_colour(v.y, false));
     } else {
       const uint64_t lo = load8(s), hi = load8(s + 8);
       store8(d + 8, s3tc_colour(hi, false));
