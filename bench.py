@@ -276,6 +276,88 @@ def run_reference_arm(args, wl_name: str, wl: dict) -> None:
     print(json.dumps(line), flush=True)
 
 
+_BATCH_IMAGES: dict = {}
+
+
+def _batch_images(wl_name: str, wl: dict, worker: int, nworkers: int, budget: int):
+    """The images one reference-arm worker compresses: every nworkers-th
+    level of the batched workload until `budget` texels (a band of rows when
+    one image is larger)."""
+    key = (wl_name, worker, nworkers)
+    if key in _BATCH_IMAGES:
+        return _BATCH_IMAGES[key]
+    from s2tc_gb300 import workloads
+    picked, tex = [], 0
+    if wl["gen"] == "mips":
+        textures = workloads.mip_textures(wl["seed"], count=wl["count"], lo=4, hi=2048)
+        levels = [(t["srccomps"], t["fmt"], lvl) for t in textures for lvl in t["levels"]]
+        for k in range(worker, len(levels), nworkers):
+            sc, fmt, lvl = levels[k]
+            picked.append((sc, fmt, np.ascontiguousarray(lvl)))
+            tex += lvl.shape[0] * lvl.shape[1]
+            if tex >= budget:
+                break
+    else:
+        img = workloads.normal_map(wl["seed"] + worker % wl["distinct"], wl["w"], wl["h"])
+        rows = max(4, (budget // wl["w"]) & ~3)
+        picked.append((3, wl["fmt"], np.ascontiguousarray(img[:rows])))
+    _BATCH_IMAGES[key] = picked
+    return picked
+
+
+def _batch_worker(args):
+    """One reference-arm step of a worker: its images through the CPU
+    encoder (knobs and rand() seeded per worker); returns (seconds, texels)."""
+    wl_name, worker, nworkers, use_ref, seed, budget = args
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    wl = WORKLOADS[wl_name]
+    imgs = _batch_images(wl_name, wl, worker, nworkers, budget)
+    enc = pyoracle.Reference() if use_ref else pyoracle.Oracle()
+    pyoracle.srand(seed * 1009 + worker)
+    t0 = time.perf_counter()
+    tex = 0
+    for sc, fmt, img in imgs:
+        h, w = img.shape[:2]
+        enc.compress(sc, w, h, img.reshape(-1), fmt, wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+        tex += w * h
+    return time.perf_counter() - t0, tex, os.getpid()
+
+
+def run_reference_arm_batch(args, wl_name: str, wl: dict) -> None:
+    """The reference's CPU encoder on a batched workload: one process per host
+    core, each compressing its own share of the images (a bounded sample)."""
+    import multiprocessing as mp
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    use_ref, kind = reference_kind()
+    cores = os.cpu_count() or 1
+    budget = 400_000
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        times, texels = [], 0
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_batch_worker, [(wl_name, k, cores, use_ref, step, budget) for k in range(cores)],
+                           chunksize=1)
+            wall = time.perf_counter() - t0
+            if step >= args.warmup:
+                concurrent = len({r[2] for r in res}) == cores
+                times.append(max(r[0] for r in res) if concurrent else wall)
+                texels = sum(r[1] for r in res)
+    total = sum(times)
+    value = texels * len(times) / total
+    sample = (f"{cores} processes, each its share of the workload's images up to {budget} texels "
+              f"({texels} texels per step)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "config": config_dict(wl_name, wl),
+            "cpu_baseline": {"value": value, "unit": "texels/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "texels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def cpu_baseline_port(wl_name: str, wl: dict, gpu_out0: np.ndarray | None) -> dict:
     """The CPU port on one core, on the full first workload image."""
     import multiprocessing as mp
@@ -753,6 +835,22 @@ def run_serving_workload(args, wl_name: str, wl: dict) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------- multi-rank
+
+def aggregate_ranks(seconds: float, units: int, dist=None, device: str = "cpu"):
+    """Replicas: every rank processed `units` in `seconds`; the job took the
+    slowest rank's time and processed all ranks' units.  Returns
+    (max seconds over ranks, units of all ranks / that time)."""
+    world = 1
+    if dist is not None and dist.is_initialized():
+        import torch
+        world = dist.get_world_size()
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        seconds = float(t.item())
+    return seconds, world * units / seconds
+
+
 # ------------------------------------------------------------------- GPU arm
 
 def main() -> None:
@@ -769,8 +867,11 @@ def main() -> None:
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
-        if wl["gen"] in ("mips", "serving", "normal_batch", "tool"):
-            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times single-image workloads"}))
+        if wl["gen"] in ("mips", "normal_batch"):
+            run_reference_arm_batch(args, args.workload, wl)
+            return
+        if wl["gen"] in ("serving", "tool"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the encoder workloads"}))
             return
         run_reference_arm(args, args.workload, wl)
         return
@@ -856,11 +957,7 @@ def main() -> None:
     s2.set_timing(False)
     s2.gpu_synchronize(sp)
     elapsed = ev0.elapsed_time(ev1) / 1000.0
-    if dist is not None:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = world * args.steps * npx / elapsed
+    elapsed, value = aggregate_ranks(elapsed, args.steps * npx, dist, "cuda")
 
     # --- end to end through tx_compress_dxtn with pinned host buffers
     e2e = None
@@ -877,11 +974,8 @@ def main() -> None:
             lib.tx_compress_dxtn(sc, w, h, h_src[i % NIMG].data_ptr(), fmt, h_dst.data_ptr(), 0)
         t_e2e = time.perf_counter() - t0
         barrier()
-        if dist is not None:
-            t = torch.tensor([t_e2e], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            t_e2e = float(t.item())
-        e2e = {"value": world * args.steps * npx / t_e2e, "unit": "texels/s",
+        t_e2e, e2e_value = aggregate_ranks(t_e2e, args.steps * npx, dist, "cuda")
+        e2e = {"value": e2e_value, "unit": "texels/s",
                "h2d_bytes_per_step": npx * sc, "d2h_bytes_per_step": out_bytes,
                "ms_per_step": 1000 * t_e2e / args.steps}
 

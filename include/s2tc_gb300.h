@@ -186,6 +186,18 @@ int s2tc_gpu_stage_ms(float *dither_ms, float *encode_ms, long long *calls);
 /* Number of CUDA kernels this library has launched since it was loaded. */
 long long s2tc_gpu_kernel_launches(void);
 
+/* The per-block encoder that s2tc_encode_block_func(dxt, colordist, nrandom,
+ * refine) selects (s2tc_algorithm.h:65-66, s2tc_algorithm.cpp:1110-1194),
+ * over every 4x4 block of a device-resident texel image in the layout
+ * rgb565_image produces (one word r | g<<8 | b<<16 | a<<24 per texel, rows of
+ * `width` words): the batched form of that per-block function.  Blocks are
+ * encoded as tx_compress_dxtn's block loop encodes them (edge blocks of
+ * min(4, width - x) x min(4, height - y) texels); block rows go `dst_pitch`
+ * bytes apart.  RANDOM_COLORS > 0 draws libc rand() on the host unless
+ * `d_rand` supplies the replayed words.  Asynchronous on `stream`. */
+int s2tc_gpu_encode_blocks(const void *d_t565, int width, int height, int dxt, int colordist, int nrandom,
+			   int refine, void *d_dst, long long dst_pitch, const unsigned int *d_rand, void *stream);
+
 /* Compress one device-resident image without allocating any memory.  No
  * counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc (engines whose frame budget or memory pool forbids allocator

@@ -137,6 +137,8 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_server_stats.restype = c_int
     lib.s2tc_server_destroy.argtypes = [vp]
     lib.s2tc_server_destroy.restype = None
+    lib.s2tc_gpu_encode_blocks.argtypes = [vp, c_int, c_int, c_int, c_int, c_int, c_int, vp, c_ll, vp, vp]
+    lib.s2tc_gpu_encode_blocks.restype = c_int
     lib.s2tc_dds_size.argtypes = [c_int, c_int, c_uint]
     lib.s2tc_dds_size.restype = c_ll
     lib.s2tc_compress_dds.argtypes = [vp, c_int, c_int, c_uint, ctypes.POINTER(Options), vp, c_ll,
@@ -166,7 +168,7 @@ EXPORTED_SYMBOLS = (
     "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
     "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit",
     "s2tc_server_wait", "s2tc_server_stats", "s2tc_server_destroy",
-    "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
+    "s2tc_gpu_encode_blocks", "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
     "s2tc_gpu_from_s3tc", "s2tc_from_s3tc_dds",
     "s2tc_last_error",
 )
@@ -426,6 +428,17 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def gpu_encode_blocks(d_t565, width: int, height: int, dxt: int, colordist: int, nrandom: int, refine: int, d_dst,
+                      dst_pitch: int = 0, d_rand=None, stream: int | None = None) -> None:
+    """``s2tc_gpu_encode_blocks``: the per-block encoder over a texel-word image."""
+    if dst_pitch == 0:
+        dst_pitch = ((width + 3) // 4) * (8 if dxt == 0 else 16)
+    st = load().s2tc_gpu_encode_blocks(_addr(d_t565), width, height, dxt, colordist, nrandom, refine, _addr(d_dst),
+                                       dst_pitch, None if d_rand is None else _addr(d_rand), stream)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_gpu_encode_blocks failed ({st}): {last_error()}")
 
 
 # ------------------------------------------------------- the reference's tools

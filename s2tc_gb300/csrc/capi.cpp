@@ -178,41 +178,14 @@ int rand_per_block(const s2tc_options& o, int dxt) {
 // order, into pinned memory, then to the device.
 constexpr long long kRandChunkWords = 1ll << 24;
 
-// `carry` (device int, may be null): the second alpha endpoint that the
-// previous call's last block left behind.  The reference encodes every block
-// of every call in the same stack frame, and a DXT5 image whose first block
-// has a single texel (a 1x1 image, e.g. the last level of a mip chain) reads
-// its second alpha candidate from that frame without writing it first
-// (s2tc_algorithm.cpp:996-1001), i.e. it sees the previous call's leftover.
-// All-texel DXT5 calls read and update it; other calls leave it alone.
-int compress_device_locked(Context& c, int srccomps, int width, int height, const uint8_t* d_src, int dxt,
-                           uint8_t* d_dst, long long pitch, const s2tc_options& opt, const unsigned int* d_rand,
-                           cudaStream_t s, int* carry = nullptr) {
-  const int sc = srccomps == 3 ? 3 : 4;
-  const long long npx = (long long)width * height;
+// Encodes every block of a texel-word image (the encoder half of a call):
+// one launch, or chunks of block rows when rand() words are replayed on the
+// host.  See compress_device_locked for `carry`.
+int encode_locked(Context& c, const uint32_t* t565, int width, int height, int dxt, uint8_t* d_dst, long long pitch,
+                  const s2tc_options& opt, const unsigned int* d_rand, cudaStream_t s, int* carry) {
   const int bw = (width + 3) / 4, bh = (height + 3) / 4;
-  if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return ST_OUT_OF_MEMORY;
-  size_t scratch = dither_scratch_bytes(npx);
-  if (opt.dither == DI_FLOYDSTEINBERG) scratch = dither_fs_scratch_bytes(width, height);
-  if (!c.scratch.reserve(scratch, "cudaMalloc(scratch)")) return ST_OUT_OF_MEMORY;
-  // the arena may still be in use by work on another stream
-  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return ST_CUDA_ERROR;
-
-  DitherArgs da{};
-  da.src = d_src;
-  da.width = width;
-  da.height = height;
-  da.srccomps = sc;
-  da.alphabits = alpha_bits(dxt);
-  da.dst = c.t565.as<uint32_t>();
-  da.error = c.err.as<int>();
-  cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
-  if (tev && !cuda_ok(cudaEventRecord(tev[0], s), "cudaEventRecord")) return ST_CUDA_ERROR;
-  if (!cuda_ok(launch_dither(da, opt.dither, c.scratch.as<uint8_t>(), s), "dither launch")) return ST_CUDA_ERROR;
-  if (tev && !cuda_ok(cudaEventRecord(tev[1], s), "cudaEventRecord")) return ST_CUDA_ERROR;
-
   EncodeArgs ea{};
-  ea.t565 = c.t565.as<uint32_t>();
+  ea.t565 = t565;
   ea.width = width;
   ea.height = height;
   ea.bw = bw;
@@ -265,6 +238,44 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
       if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
     }
   }
+  return ST_OK;
+}
+
+// `carry` (device int, may be null): the second alpha endpoint that the
+// previous call's last block left behind.  The reference encodes every block
+// of every call in the same stack frame, and a DXT5 image whose first block
+// has a single texel (a 1x1 image, e.g. the last level of a mip chain) reads
+// its second alpha candidate from that frame without writing it first
+// (s2tc_algorithm.cpp:996-1001), i.e. it sees the previous call's leftover.
+// All-texel DXT5 calls read and update it; other calls leave it alone.
+int compress_device_locked(Context& c, int srccomps, int width, int height, const uint8_t* d_src, int dxt,
+                           uint8_t* d_dst, long long pitch, const s2tc_options& opt, const unsigned int* d_rand,
+                           cudaStream_t s, int* carry = nullptr) {
+  const int sc = srccomps == 3 ? 3 : 4;
+  const long long npx = (long long)width * height;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4;
+  if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return ST_OUT_OF_MEMORY;
+  size_t scratch = dither_scratch_bytes(npx);
+  if (opt.dither == DI_FLOYDSTEINBERG) scratch = dither_fs_scratch_bytes(width, height);
+  if (!c.scratch.reserve(scratch, "cudaMalloc(scratch)")) return ST_OUT_OF_MEMORY;
+  // the arena may still be in use by work on another stream
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return ST_CUDA_ERROR;
+
+  DitherArgs da{};
+  da.src = d_src;
+  da.width = width;
+  da.height = height;
+  da.srccomps = sc;
+  da.alphabits = alpha_bits(dxt);
+  da.dst = c.t565.as<uint32_t>();
+  da.error = c.err.as<int>();
+  cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
+  if (tev && !cuda_ok(cudaEventRecord(tev[0], s), "cudaEventRecord")) return ST_CUDA_ERROR;
+  if (!cuda_ok(launch_dither(da, opt.dither, c.scratch.as<uint8_t>(), s), "dither launch")) return ST_CUDA_ERROR;
+  if (tev && !cuda_ok(cudaEventRecord(tev[1], s), "cudaEventRecord")) return ST_CUDA_ERROR;
+
+  const int st = encode_locked(c, c.t565.as<uint32_t>(), width, height, dxt, d_dst, pitch, opt, d_rand, s, carry);
+  if (st != ST_OK) return st;
   if (tev) {
     if (!cuda_ok(cudaEventRecord(tev[2], s), "cudaEventRecord")) return ST_CUDA_ERROR;
     c.timed_calls++;
@@ -804,6 +815,34 @@ int s2tc_gpu_compress(int srccomps, int width, int height, const void* d_src, un
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
   return compress_device_locked(c, srccomps, width, height, static_cast<const uint8_t*>(d_src), dxt,
                                 static_cast<uint8_t*>(d_dst), dst_pitch, normalise(*opt), d_rand, s);
+}
+
+int s2tc_gpu_encode_blocks(const void* d_t565, int width, int height, int dxt, int colordist, int nrandom, int refine,
+                           void* d_dst, long long dst_pitch, const unsigned int* d_rand, void* stream) {
+  if (dxt < s2tc::DXT1 || dxt > s2tc::DXT5) {
+    set_error("bad DxtMode");
+    return S2TC_ERR_FORMAT;
+  }
+  if (width < 0 || height < 0 || (width > 0 && height > 0 && (!d_t565 || !d_dst))) {
+    set_error("bad argument");
+    return S2TC_ERR_ARGUMENT;
+  }
+  if (width == 0 || height == 0) return S2TC_OK;
+  if (dst_pitch < (long long)((width + 3) / 4) * s2tc::block_bytes(dxt)) {
+    set_error("dst_pitch smaller than a block row");
+    return S2TC_ERR_ARGUMENT;
+  }
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+  const s2tc_options o = normalise(s2tc_options{s2tc::DI_NONE, colordist, nrandom, refine});
+  // host-replayed rand() words go through the arena's staging buffers
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return S2TC_ERR_CUDA;
+  const int st = encode_locked(c, static_cast<const uint32_t*>(d_t565), width, height, dxt,
+                               static_cast<uint8_t*>(d_dst), dst_pitch, o, d_rand, s, nullptr);
+  if (st != S2TC_OK) return st;
+  return cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord") ? S2TC_OK : S2TC_ERR_CUDA;
 }
 
 int s2tc_gpu_synchronize(void* stream) {

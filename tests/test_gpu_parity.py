@@ -335,3 +335,22 @@ def test_random_candidates_repeated_values(lib, oracle, metric):
                 a = gpu_compress(4, w, h, img, fmt, 0, metric, nr, refine, 5)
                 b = oracle.compress(4, w, h, img, fmt, 0, metric, nr, refine, seed=5)
                 assert np.array_equal(a, b), (hex(fmt), kind, nr)
+
+
+def test_gpu_encode_blocks(lib, oracle):
+    """The batched per-block entry point on texel words equals the encoder
+    half of tx_compress_dxtn (dither NONE makes the texel words known)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    for dxt, fmt, abits in ((0, 0x83F1, 1), (1, 0x83F2, 4), (2, 0x83F3, 8)):
+        for metric, nr, refine in ((5, -1, 1), (3, 0, 2), (7, 16, 2), (2, 0, 0), (1, 40, 1)):
+            for w, h in ((1, 1), (int(rng.integers(2, 60)), int(rng.integers(2, 60)))):
+                img = cases.image(rng, w, h, 4)
+                t565 = oracle.rgb565_image(img, w, h, 4, abits, 0)
+                d_t = torch.from_numpy(t565).cuda()
+                d_out = torch.zeros(s2.compressed_size(w, h, fmt), dtype=torch.uint8, device="cuda")
+                pyoracle.srand(5)
+                s2.gpu_encode_blocks(d_t, w, h, dxt, metric, nr, refine, d_out)
+                s2.gpu_synchronize(None)
+                want = oracle.compress(4, w, h, img, fmt, 0, metric, nr, refine, seed=5)
+                assert np.array_equal(d_out.cpu().numpy(), want), (dxt, metric, nr, refine, w, h)
