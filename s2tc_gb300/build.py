@@ -40,7 +40,7 @@ def _units():
     units = []
     for m in range(N_METRICS):
         units.append((CSRC / "encode.cu", OBJ_DIR / f"encode_m{m}.o", [f"-DS2TC_METRIC={m}"]))
-    for name in ("dither.cu", "dither_fs.cu", "noalloc.cu", "tools.cu"):
+    for name in ("dither.cu", "dither_fs.cu", "noalloc.cu", "tools.cu", "rand_glibc.cu"):
         units.append((CSRC / name, OBJ_DIR / (Path(name).stem + ".o"), []))
     units.append((CSRC / "capi.cpp", OBJ_DIR / "capi.o", ["-x", "cu"]))
     units.append((CSRC / "server.cpp", OBJ_DIR / "server.o", ["-x", "cu"]))

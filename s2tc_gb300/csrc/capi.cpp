@@ -21,6 +21,7 @@
 
 #include "dither.h"
 #include "encode.h"
+#include "rand_glibc.h"
 #include "tools.h"
 #include "s2tc_types.h"
 
@@ -88,6 +89,7 @@ struct Context {
   long long timed_calls = 0;
   DevBuf src, t565, dst, scratch, rnd, err;
   DevBuf mips, blocks;  // s2tc_compress_dds: every level's pixels and blocks
+  DevBuf rnd_win;       // the rand() stream position for the device generator
   PinnedBuf host_rnd, host_out;
 
   bool init() {
@@ -178,6 +180,7 @@ int rand_per_block(const s2tc_options& o, int dxt) {
 // order, into pinned memory, then to the device.
 constexpr long long kRandChunkWords = 1ll << 24;
 
+
 // Encodes every block of a texel-word image (the encoder half of a call):
 // one launch, or chunks of block rows when rand() words are replayed on the
 // host.  See compress_device_locked for `carry`.
@@ -208,6 +211,25 @@ int encode_locked(Context& c, const uint32_t* t565, int width, int height, int d
     ea.by0 = 0;
     ea.nby = bh;
     ea.rnd = nullptr;
+    if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
+  } else if (!d_rand && (long long)bw * bh * per_block >= kRandDeviceMin && rand_usable()) {
+    // libc's rand() stream generated on the GPU from its current position
+    // (libc's state jumps ahead by the words taken)
+    const long long words = (long long)bw * bh * per_block;
+    RandWindow win;
+    if (!c.rnd.reserve(size_t(words) * 4, "cudaMalloc(rand)")) return ST_OUT_OF_MEMORY;
+    if (!c.rnd_win.reserve(sizeof(RandWindow), "cudaMalloc(rand window)")) return ST_OUT_OF_MEMORY;
+    if (!rand_take(words, &win)) {
+      set_error("libc rand() state could not be read");
+      return ST_CUDA_ERROR;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(c.rnd_win.p, &win, sizeof(win), cudaMemcpyHostToDevice, s), "rand window upload"))
+      return ST_CUDA_ERROR;
+    if (!cuda_ok(rand_fill(c.rnd_win.as<RandWindow>(), c.rnd.as<uint32_t>(), words, s), "rand fill"))
+      return ST_CUDA_ERROR;
+    ea.by0 = 0;
+    ea.nby = bh;
+    ea.rnd = c.rnd.as<uint32_t>();
     if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, s), "encode launch")) return ST_CUDA_ERROR;
   } else {
     // block rows in chunks so the replayed rand words stay bounded (one
@@ -351,6 +373,8 @@ struct Batch {
   DevBuf t565, scratch, tables, rnd;
   PinnedBuf host_rnd;
   long long host_rand_words = 0;        // rand words replayed per run (host path)
+  bool device_rand = false;             // ... generated on the device from a pinned window
+  DevBuf rnd_win;
   std::vector<long long> rand_words;    // per image
   cudaStream_t capture = nullptr;
   cudaGraph_t graph = nullptr;
@@ -369,7 +393,7 @@ struct Batch {
     if (graph) cudaGraphDestroy(graph);
     if (done) cudaEventDestroy(done);
     if (capture) cudaStreamDestroy(capture);
-    for (DevBuf* b : {&t565, &scratch, &tables, &rnd})
+    for (DevBuf* b : {&t565, &scratch, &tables, &rnd, &rnd_win})
       if (b->p) cudaFree(b->p);
     if (host_rnd.p) cudaFreeHost(host_rnd.p);
   }
@@ -518,7 +542,13 @@ int batch_prepare(Batch& b, Context& c) {
 // The launch sequence of a batch on stream `s` (captured once into the graph).
 int batch_launch(Batch& b, cudaStream_t s) {
   const long long l0 = launches_so_far();
-  if (b.host_rand_words > 0) {
+  if (b.host_rand_words > 0 && b.device_rand) {
+    if (!cuda_ok(cudaMemcpyAsync(b.rnd_win.p, b.host_rnd.p, sizeof(RandWindow), cudaMemcpyHostToDevice, s),
+                 "batch rand window upload"))
+      return ST_CUDA_ERROR;
+    if (!cuda_ok(rand_fill(b.rnd_win.as<RandWindow>(), b.rnd.as<uint32_t>(), b.host_rand_words, s), "rand fill"))
+      return ST_CUDA_ERROR;
+  } else if (b.host_rand_words > 0) {
     if (!cuda_ok(cudaMemcpyAsync(b.rnd.p, b.host_rnd.p, size_t(b.host_rand_words) * 4, cudaMemcpyHostToDevice, s),
                  "batch rand upload"))
       return ST_CUDA_ERROR;
@@ -951,8 +981,13 @@ int s2tc_batch_create(s2tc_batch** out, const s2tc_image* items, int count, cons
       b.host_rand_words += im.rand ? 0 : words;
     }
     if (b.host_rand_words > 0) {
+      // the words come from the device generator (a pinned window per run)
+      // unless libc's state cannot be read
+      b.device_rand = s2tc::rand_usable() && cuda_ok(s2tc::rand_prepare(), "rand table upload");
+      const size_t staging = b.device_rand ? sizeof(s2tc::RandWindow) : size_t(b.host_rand_words) * 4;
       if (!b.rnd.reserve(size_t(b.host_rand_words) * 4, "cudaMalloc(batch rand)") ||
-          !b.host_rnd.reserve(size_t(b.host_rand_words) * 4, "cudaMallocHost(batch rand)")) {
+          !b.host_rnd.reserve(staging, "cudaMallocHost(batch rand)") ||
+          (b.device_rand && !b.rnd_win.reserve(sizeof(s2tc::RandWindow), "cudaMalloc(rand window)"))) {
         delete h;
         return S2TC_ERR_NOMEM;
       }
@@ -1002,8 +1037,14 @@ int s2tc_batch_run(s2tc_batch* h, void* stream) {
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
   // a previous run of this plan must be done with the staging and scratch
   if (!cuda_ok(cudaEventSynchronize(b.done), "cudaEventSynchronize")) return S2TC_ERR_CUDA;
-  if (b.host_rand_words > 0) {
-    // libc rand() in image order, exactly as one tx_compress_dxtn call per image would draw it
+  if (b.host_rand_words > 0 && b.device_rand) {
+    // libc rand() in image order, exactly as one tx_compress_dxtn call per
+    // image would draw it: the stream's position now, generated on the device
+    if (!s2tc::rand_take(b.host_rand_words, static_cast<s2tc::RandWindow*>(b.host_rnd.p))) {
+      set_error("libc rand() state could not be read");
+      return S2TC_ERR_CUDA;
+    }
+  } else if (b.host_rand_words > 0) {
     unsigned int* hr = static_cast<unsigned int*>(b.host_rnd.p);
     for (long long i = 0; i < b.host_rand_words; ++i) hr[i] = unsigned(std::rand());
   }

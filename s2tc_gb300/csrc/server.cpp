@@ -29,6 +29,7 @@
 
 #include "dither.h"
 #include "encode.h"
+#include "rand_glibc.h"
 #include "s2tc_gb300.h"
 #include "s2tc_types.h"
 
@@ -117,7 +118,9 @@ struct Req {
   long long dpitch = 0;
   long long npx = 0, bw = 0, bh = 0;
   size_t in_bytes = 0, tex_bytes = 0, out_bytes = 0, rand_bytes = 0, total = 0;
-  std::vector<unsigned> rand;  // replayed rand() words (random-candidate mode)
+  std::vector<unsigned> rand;  // replayed rand() words (random-candidate mode, host loop)
+  RandWindow win{};            // or the stream position they start at (device generator)
+  bool dev_rand = false;
   size_t off = 0;              // pool allocation
   double t_submit = 0, t_done = 0;
   int status = 1;              // 1 pending, 0 done, < 0 error
@@ -175,7 +178,7 @@ int launch_round(s2tc_server* sv, Slot& sl) {
   for (auto& r : rs) {
     if (cudaMemcpyAsync(base + r->off, r->hsrc, r->in_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
       return S2TC_ERR_CUDA;
-    if (r->rand_bytes &&
+    if (r->rand_bytes && !r->dev_rand &&
         cudaMemcpyAsync(base + r->off + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign) +
                             align_up(r->out_bytes, kAlign),
                         r->rand.data(), r->rand_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
@@ -286,8 +289,20 @@ int launch_round(s2tc_server* sv, Slot& sl) {
     }
     launches.push_back(std::move(L));
   }
+  // rand() stream positions of the requests whose words the device generates
+  std::vector<std::pair<size_t, Req*>> gens;
+  for (auto& r : rs)
+    if (r->dev_rand) gens.emplace_back(put(&r->win, sizeof(RandWindow)), r.get());
   if (toff > sl.tab_bytes || soff > sl.scratch_bytes) return S2TC_ERR_TOO_LARGE;
   if (toff && cudaMemcpyAsync(sl.dtab, sl.htab, toff, cudaMemcpyHostToDevice, s) != cudaSuccess) return S2TC_ERR_CUDA;
+  for (auto& g : gens) {
+    Req* r = g.second;
+    uint32_t* drand = reinterpret_cast<uint32_t*>(base + r->off + align_up(r->in_bytes, kAlign) +
+                                                  align_up(r->tex_bytes, kAlign) + align_up(r->out_bytes, kAlign));
+    if (rand_fill(reinterpret_cast<const RandWindow*>(sl.dtab + g.first), drand, (long long)(r->rand_bytes / 4), s) !=
+        cudaSuccess)
+      return S2TC_ERR_CUDA;
+  }
   for (Launch& L : launches) {
     if (L.dither == DI_FLOYDSTEINBERG) {
       for (size_t i = 0; i < L.fs.size(); ++i)
@@ -409,7 +424,8 @@ int s2tc_server_create(s2tc_server** out, long long budget_bytes) {
             cudaStreamCreateWithFlags(&sv->copy_in, cudaStreamNonBlocking) == cudaSuccess &&
             cudaStreamCreateWithFlags(&sv->copy_out, cudaStreamNonBlocking) == cudaSuccess;
   // per-slot tables and scan scratch (outside the request budget)
-  const size_t tab = size_t(s2tc::kMaxRoundRequests) * 4 * (sizeof(s2tc::EncodeArgs) + sizeof(s2tc::DitherItem) + 64);
+  const size_t tab = size_t(s2tc::kMaxRoundRequests) *
+                     (4 * (sizeof(s2tc::EncodeArgs) + sizeof(s2tc::DitherItem) + 64) + sizeof(s2tc::RandWindow) + 16);
   const size_t scratch = size_t(64) << 20;
   for (int k = 0; k < s2tc::kSlots && ok; ++k) {
     s2tc::Slot& sl = sv->slots[k];
@@ -464,8 +480,13 @@ int s2tc_server_submit(s2tc_server* sv, const void* src, int srccomps, int width
   if (normal && r->opt.nrandom > 0) {
     // libc rand() drawn now, in submission order, as tx_compress_dxtn would
     const size_t words = size_t(r->bw * r->bh) * r->opt.nrandom * (dxt == s2tc::DXT5 ? 4 : 3);
-    r->rand.resize(words);
-    for (size_t i = 0; i < words; ++i) r->rand[i] = unsigned(std::rand());
+    if ((long long)words >= kRandDeviceMin && rand_usable() && rand_prepare() == cudaSuccess &&
+        rand_take((long long)words, &r->win)) {
+      r->dev_rand = true;  // generated on the device when its round launches
+    } else {
+      r->rand.resize(words);
+      for (size_t i = 0; i < words; ++i) r->rand[i] = unsigned(std::rand());
+    }
     r->rand_bytes = words * 4;
   }
   r->total = align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign) + align_up(r->out_bytes, kAlign) +

@@ -354,3 +354,21 @@ def test_gpu_encode_blocks(lib, oracle):
                 s2.gpu_synchronize(None)
                 want = oracle.compress(4, w, h, img, fmt, 0, metric, nr, refine, seed=5)
                 assert np.array_equal(d_out.cpu().numpy(), want), (dxt, metric, nr, refine, w, h)
+
+
+def test_device_rand_stream_continues(lib, oracle):
+    """Large random-candidate calls take libc's rand() words on the GPU: the
+    bytes equal the oracle's (which calls rand() itself) and the process's
+    rand() stream continues exactly after the words consumed."""
+    img = workloads.plain_rgba(8, 384, 256).reshape(-1)
+    for fmt, nr in ((0x83F1, 64), (0x83F3, 9)):
+        words = s2.rand_words(384, 256, fmt, s2.options(1, 5, nr, 1))
+        assert words >= 16384
+        a = gpu_compress(4, 384, 256, img, fmt, 1, 5, nr, 1, seed=31)
+        after = pyoracle.libc_rand()
+        b = oracle.compress(4, 384, 256, img, fmt, 1, 5, nr, 1, seed=31)
+        assert np.array_equal(a, b), hex(fmt)
+        pyoracle.srand(31)
+        for _ in range(words):
+            pyoracle.libc_rand()
+        assert after == pyoracle.libc_rand()

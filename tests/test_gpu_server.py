@@ -49,6 +49,29 @@ def test_server_matches_requests_alone(lib):
         assert np.array_equal(got.numpy(), want), (w, h, hex(fmt), opt.metric, opt.nrandom)
 
 
+def test_server_random_candidates(lib):
+    """Random-candidate requests large enough for the device generator: the
+    words each request draws at submit time, in order, match one
+    tx_compress_dxtn call per request in the same order."""
+    torch = pytest.importorskip("torch")
+    srv = s2.Server(1 << 30)
+    reqs = []
+    for k, (w, h, fmt) in enumerate([(256, 192, 0x83F1), (64, 64, 0x83F3), (300, 200, 0x83F3), (128, 512, 0x83F1)]):
+        img = workloads.plain_rgba(60 + k, w, h).reshape(-1)
+        dst = torch.zeros(s2.compressed_size(w, h, fmt), dtype=torch.uint8).pin_memory()
+        reqs.append((img, w, h, fmt, dst))
+    opt = s2.options(1, s2.WAVG, 32, 1)
+    pyoracle.srand(77)
+    ids = [srv.submit(torch.from_numpy(img).pin_memory(), 4, w, h, fmt, opt, dst) for img, w, h, fmt, dst in reqs]
+    for i in ids:
+        srv.wait(i)
+    srv.close()
+    s2.set_env(1, s2.WAVG, 32, 1)
+    pyoracle.srand(77)
+    for img, w, h, fmt, dst in reqs:
+        assert np.array_equal(dst.numpy(), s2.tx_compress_dxtn(4, w, h, img, fmt)), (w, h, hex(fmt))
+
+
 def test_server_budget_admission(lib):
     """A small budget admits requests as memory frees up (several rounds, the
     pool never above the budget); a request above the budget is refused."""
