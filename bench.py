@@ -382,7 +382,11 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     from s2tc_gb300 import workloads
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     opt = s2.options(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
-    if wl["gen"] == "mips":
+    layouts = {}
+    if not args.no_autotune:
+        for f in ((0x83F1, 0x83F2, 0x83F3) if wl["gen"] == "mips" else (wl["fmt"],)):
+            s2.autotune(opt, f, 1024, 1024)
+            layouts[FMT_NAMES[f]] = s2.get_layout(opt, f)
         tex = workloads.mip_textures(wl["seed"], count=wl["count"], lo=4, hi=2048)
         levels = [(t, lvl) for t in tex for lvl in t["levels"]]
     else:
@@ -506,7 +510,8 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t_batch / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": dict(config_dict(wl_name, wl), images=len(images), texels=texels),
+            "config": dict(config_dict(wl_name, wl), images=len(images), texels=texels,
+                           launch_layout=layouts or "default"),
             "per_image": {"value": single, "unit": "texels/s", "ms_per_step": 1000 * t_single / args.steps,
                           "launches_per_step": None},
             "batched_over_per_image": value / single, "bit_exact_batched_vs_per_image": bit_exact,
@@ -868,6 +873,7 @@ def main() -> None:
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU port leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch layouts")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.warmup < 3 and args.impl == "gb300":
@@ -915,6 +921,10 @@ def main() -> None:
     npx = w * h
     out_bytes = s2.compressed_size(w, h, fmt)
     opt = s2.options(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+    layout = None
+    if not args.no_autotune:
+        s2.autotune(opt, fmt, min(w, 2048), min(h, 2048))
+        layout = s2.get_layout(opt, fmt)
     images = [make_image(wl, wl["seed"] + 100 * rank + i) for i in range(NIMG)]
     d_src = [torch.from_numpy(im).cuda() for im in images]
     d_dst = [torch.empty(out_bytes, dtype=torch.uint8, device="cuda") for _ in range(NIMG)]
@@ -1020,7 +1030,8 @@ def main() -> None:
         line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-                "config": config_dict(args.workload, wl), "e2e": e2e, "gpu_launches": launches,
+                "config": dict(config_dict(args.workload, wl), launch_layout=layout or "default"),
+                "e2e": e2e, "gpu_launches": launches,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
         print(json.dumps(line), flush=True)

@@ -213,6 +213,21 @@ int s2tc_gpu_compress_noalloc(int srccomps, int width, int height, const void *d
 			      void *d_dst, long long dst_pitch, const s2tc_options *opt, const unsigned int *d_rand,
 			      void *stream);
 
+/* Launch layout of the encoder for one mode (format, colour distance,
+ * RANDOM_COLORS > 0 / = 0 / quick, refinement): threads per CTA of the
+ * thread-per-block kernels (32..128), and warps per CTA (1..4) and CTAs per
+ * SM of the random-candidate kernel's persistent grid.  No counterpart in the
+ * reference: layouts change speed only, never bytes.  s2tc_autotune times
+ * the candidate layouts of a mode on a synthetic width x height image (it
+ * does not consume libc rand()) and keeps the fastest for the rest of the
+ * process; `best_ms` (may be NULL) receives that layout's encoder time.
+ * s2tc_encode_layout_set sets one by hand. */
+int s2tc_autotune(const s2tc_options *opt, unsigned int format, int width, int height, float *best_ms);
+int s2tc_encode_layout_set(const s2tc_options *opt, unsigned int format, int threads, int rand_warps,
+			   int rand_ctas_per_sm);
+int s2tc_encode_layout_get(const s2tc_options *opt, unsigned int format, int *threads, int *rand_warps,
+			   int *rand_ctas_per_sm);
+
 /* ---------------------------------------------------------------------
  * Part 3: the reference's command-line tools, in memory, on the GPU.
  * --------------------------------------------------------------------- */

@@ -139,6 +139,13 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_server_destroy.restype = None
     lib.s2tc_gpu_encode_blocks.argtypes = [vp, c_int, c_int, c_int, c_int, c_int, c_int, vp, c_ll, vp, vp]
     lib.s2tc_gpu_encode_blocks.restype = c_int
+    lib.s2tc_autotune.argtypes = [ctypes.POINTER(Options), c_uint, c_int, c_int, ctypes.POINTER(ctypes.c_float)]
+    lib.s2tc_autotune.restype = c_int
+    lib.s2tc_encode_layout_set.argtypes = [ctypes.POINTER(Options), c_uint, c_int, c_int, c_int]
+    lib.s2tc_encode_layout_set.restype = c_int
+    lib.s2tc_encode_layout_get.argtypes = [ctypes.POINTER(Options), c_uint, ctypes.POINTER(c_int),
+                                           ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
+    lib.s2tc_encode_layout_get.restype = c_int
     lib.s2tc_dds_size.argtypes = [c_int, c_int, c_uint]
     lib.s2tc_dds_size.restype = c_ll
     lib.s2tc_compress_dds.argtypes = [vp, c_int, c_int, c_uint, ctypes.POINTER(Options), vp, c_ll,
@@ -168,7 +175,7 @@ EXPORTED_SYMBOLS = (
     "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
     "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit",
     "s2tc_server_wait", "s2tc_server_stats", "s2tc_server_destroy",
-    "s2tc_gpu_encode_blocks", "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
+    "s2tc_gpu_encode_blocks", "s2tc_autotune", "s2tc_encode_layout_set", "s2tc_encode_layout_get", "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
     "s2tc_gpu_from_s3tc", "s2tc_from_s3tc_dds",
     "s2tc_last_error",
 )
@@ -439,6 +446,28 @@ def gpu_encode_blocks(d_t565, width: int, height: int, dxt: int, colordist: int,
                                        dst_pitch, None if d_rand is None else _addr(d_rand), stream)
     if st != S2TC_OK:
         raise S2tcError(f"s2tc_gpu_encode_blocks failed ({st}): {last_error()}")
+
+
+def autotune(opt: Options, fmt: int, width: int = 1024, height: int = 1024) -> float:
+    """``s2tc_autotune``: keeps the fastest launch layout for this mode;
+    returns its encoder time in ms."""
+    ms = ctypes.c_float()
+    st = load().s2tc_autotune(ctypes.byref(opt), fmt, width, height, ctypes.byref(ms))
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_autotune failed ({st}): {last_error()}")
+    return ms.value
+
+
+def set_layout(opt: Options, fmt: int, threads: int = 128, rand_warps: int = 4, rand_ctas_per_sm: int = 64) -> None:
+    st = load().s2tc_encode_layout_set(ctypes.byref(opt), fmt, threads, rand_warps, rand_ctas_per_sm)
+    if st != S2TC_OK:
+        raise S2tcError(f"s2tc_encode_layout_set failed ({st}): {last_error()}")
+
+
+def get_layout(opt: Options, fmt: int) -> dict:
+    t, w, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    load().s2tc_encode_layout_get(ctypes.byref(opt), fmt, ctypes.byref(t), ctypes.byref(w), ctypes.byref(c))
+    return {"threads": t.value, "rand_warps": w.value, "rand_ctas_per_sm": c.value}
 
 
 # ------------------------------------------------------- the reference's tools

@@ -361,6 +361,28 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
 }
 
 
+// ------------------------------------------------------------ launch layouts
+
+struct LayoutTable {
+  std::mutex mu;
+  EncodeLayout t[8][3][3][3];  // metric, format, refinement, kind
+  LayoutTable() {
+    for (auto& a : t)
+      for (auto& b : a)
+        for (auto& c : b)
+          for (auto& d : c) d = EncodeLayout{128, 4, 64};
+  }
+};
+
+LayoutTable& layouts() {
+  static LayoutTable* l = new LayoutTable();
+  return *l;
+}
+
+bool layout_key_ok(int metric, int dxt, int refine, int kind) {
+  return metric >= 0 && metric < 8 && dxt >= 0 && dxt < 3 && refine >= 0 && refine < 3 && kind >= 0 && kind < 3;
+}
+
 // ------------------------------------------------------------------ batches
 
 // A planned batch: device tables, scratch and a CUDA graph of the whole
@@ -1170,6 +1192,160 @@ int s2tc_compress_dds(const void* rgba, int width, int height, unsigned int form
   return S2TC_OK;
 }
 
+int s2tc_encode_layout_set(const s2tc_options* opt, unsigned int format, int threads, int rand_warps,
+                           int rand_ctas_per_sm) {
+  using namespace s2tc;
+  const int dxt = format_dxt(format);
+  if (dxt < 0 || !opt) return S2TC_ERR_ARGUMENT;
+  if (threads < 32 || threads > 128 || rand_warps < 1 || rand_warps > 4 || rand_ctas_per_sm < 1) {
+    set_error("layout out of range (threads 32..128, warps 1..4, CTAs per SM >= 1)");
+    return S2TC_ERR_ARGUMENT;
+  }
+  const s2tc_options o = normalise(*opt);
+  const bool normal = normal_mode(o);
+  const int kind = normal ? (o.nrandom > 0 ? kLayoutRand : kLayoutFull) : kLayoutQuick;
+  set_encode_layout(o.metric, dxt, o.refine, kind, EncodeLayout{threads & ~31, rand_warps, rand_ctas_per_sm});
+  return S2TC_OK;
+}
+
+int s2tc_encode_layout_get(const s2tc_options* opt, unsigned int format, int* threads, int* rand_warps,
+                           int* rand_ctas_per_sm) {
+  using namespace s2tc;
+  const int dxt = format_dxt(format);
+  if (dxt < 0 || !opt) return S2TC_ERR_ARGUMENT;
+  const s2tc_options o = normalise(*opt);
+  const bool normal = normal_mode(o);
+  const int kind = normal ? (o.nrandom > 0 ? kLayoutRand : kLayoutFull) : kLayoutQuick;
+  const EncodeLayout L = encode_layout(o.metric, dxt, o.refine, kind);
+  if (threads) *threads = L.threads;
+  if (rand_warps) *rand_warps = L.rand_warps;
+  if (rand_ctas_per_sm) *rand_ctas_per_sm = L.rand_ctas_per_sm;
+  return S2TC_OK;
+}
+
+// Autotuner: times the candidate layouts of one mode's encoder launch on a
+// synthetic image (texel words from a fixed xorshift stream, random-candidate
+// words from the device generator started at a synthetic position, so that
+// libc's rand() is not consumed) and keeps the fastest.
+int s2tc_autotune(const s2tc_options* opt, unsigned int format, int width, int height, float* best_ms) {
+  using namespace s2tc;
+  const int dxt = format_dxt(format);
+  if (dxt < 0 || !opt || width < 4 || height < 4) {
+    set_error("bad argument");
+    return S2TC_ERR_ARGUMENT;
+  }
+  const s2tc_options o = normalise(*opt);
+  const bool normal = normal_mode(o);
+  const int kind = normal ? (o.nrandom > 0 ? kLayoutRand : kLayoutFull) : kLayoutQuick;
+  std::vector<EncodeLayout> cands;
+  if (kind == kLayoutRand) {
+    for (int wps : {1, 2, 4})
+      for (int cps : {8, 16, 32, 64}) cands.push_back(EncodeLayout{128, wps, cps});
+  } else {
+    for (int th : {32, 64, 96, 128}) cands.push_back(EncodeLayout{th, 4, 64});
+  }
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lock(c.mu);
+  if (!c.init()) return S2TC_ERR_CUDA;
+  cudaStream_t s = c.stream;
+  const long long npx = (long long)width * height;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const long long pitch = (long long)bw * block_bytes(dxt);
+  const long long words = (long long)bw * bh * rand_per_block(o, dxt);
+  std::vector<uint32_t> host(static_cast<size_t>(npx));
+  uint32_t x = 0x9E3779B9u;
+  const uint32_t amask = dxt == s2tc::DXT1 ? 1u : dxt == s2tc::DXT3 ? 15u : 255u;
+  for (long long i = 0; i < npx; ++i) {
+    x ^= x << 13;
+    x ^= x >> 17;
+    x ^= x << 5;
+    const long long px = i % width, py = i / width;
+    const bool smooth = ((px / 64) + (py / 64)) & 1;  // half the image in smooth tiles
+    const uint32_t r = smooth ? uint32_t((px / 8) & 31) : (x & 31), g = smooth ? uint32_t((py / 4) & 63) : ((x >> 5) & 63);
+    const uint32_t b = smooth ? uint32_t(((px + py) / 16) & 31) : ((x >> 11) & 31);
+    const uint32_t a = dxt == s2tc::DXT1 ? 1u : ((x >> 16) & amask);
+    host[size_t(i)] = r | (g << 8) | (b << 16) | (a << 24);
+  }
+  DevBuf tex, dst, rnd, win;
+  struct Free {
+    DevBuf* b[4];
+    ~Free() {
+      for (DevBuf* d : b)
+        if (d->p) cudaFree(d->p);
+    }
+  } cleanup{{&tex, &dst, &rnd, &win}};
+  if (!tex.reserve(size_t(npx) * 4, "cudaMalloc(autotune texels)") ||
+      !dst.reserve(size_t(pitch) * bh, "cudaMalloc(autotune blocks)"))
+    return S2TC_ERR_NOMEM;
+  if (!cuda_ok(cudaMemcpy(tex.p, host.data(), size_t(npx) * 4, cudaMemcpyHostToDevice), "autotune upload"))
+    return S2TC_ERR_CUDA;
+  if (words > 0) {
+    RandWindow w;
+    for (int i = 0; i < 61; ++i) {
+      x ^= x << 13;
+      x ^= x >> 17;
+      x ^= x << 5;
+      w.ext[i] = x;
+    }
+    if (!rnd.reserve(size_t(words) * 4, "cudaMalloc(autotune rand)") ||
+        !win.reserve(sizeof(RandWindow), "cudaMalloc(autotune window)"))
+      return S2TC_ERR_NOMEM;
+    if (!cuda_ok(cudaMemcpy(win.p, &w, sizeof(w), cudaMemcpyHostToDevice), "autotune window") ||
+        !cuda_ok(rand_fill(win.as<RandWindow>(), rnd.as<uint32_t>(), words, s), "autotune rand"))
+      return S2TC_ERR_CUDA;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (!cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&e1), "cudaEventCreate"))
+    return S2TC_ERR_CUDA;
+  float best = 0;
+  EncodeLayout best_l = cands[0];
+  int st = S2TC_OK;
+  for (const EncodeLayout& L : cands) {
+    set_encode_layout(o.metric, dxt, o.refine, kind, L);
+    float ms = 0;
+    for (int rep = 0; rep < 4 && st == S2TC_OK; ++rep) {
+      if (rep == 1 && !cuda_ok(cudaEventRecord(e0, s), "cudaEventRecord")) st = S2TC_ERR_CUDA;
+      if (st == S2TC_OK)
+        st = encode_locked(c, tex.as<uint32_t>(), width, height, dxt, dst.as<uint8_t>(), pitch, o,
+                           words > 0 ? rnd.as<uint32_t>() : nullptr, s, nullptr);
+    }
+    if (st == S2TC_OK && (!cuda_ok(cudaEventRecord(e1, s), "cudaEventRecord") ||
+                          !cuda_ok(cudaEventSynchronize(e1), "cudaEventSynchronize") ||
+                          !cuda_ok(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime")))
+      st = S2TC_ERR_CUDA;
+    if (st != S2TC_OK) break;
+    ms /= 3;
+    if (best == 0 || ms < best) {
+      best = ms;
+      best_l = L;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  set_encode_layout(o.metric, dxt, o.refine, kind, best_l);
+  if (st == S2TC_OK) st = check_error_flag(c, s);
+  if (best_ms) *best_ms = best;
+  return st;
+}
+
 const char* s2tc_last_error(void) { return s2tc::g_last_error.c_str(); }
 
 }  // extern "C"
+
+namespace s2tc {
+
+EncodeLayout encode_layout(int metric, int dxt, int refine, int kind) {
+  if (!layout_key_ok(metric, dxt, refine, kind)) return EncodeLayout{128, 4, 64};
+  LayoutTable& l = layouts();
+  std::lock_guard<std::mutex> lock(l.mu);
+  return l.t[metric][dxt][refine][kind];
+}
+
+void set_encode_layout(int metric, int dxt, int refine, int kind, EncodeLayout layout) {
+  if (!layout_key_ok(metric, dxt, refine, kind)) return;
+  LayoutTable& l = layouts();
+  std::lock_guard<std::mutex> lock(l.mu);
+  l.t[metric][dxt][refine][kind] = layout;
+}
+
+}  // namespace s2tc

@@ -834,7 +834,8 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
   const int stride = DXT == DXT5 ? 4 : 3;
   const long long nb = w.total;
 
-  for (long long g = (long long)blockIdx.x * kRandWarps + warp; g < nb; g += (long long)gridDim.x * kRandWarps) {
+  const int warps = int(blockDim.x >> 5);
+  for (long long g = (long long)blockIdx.x * warps + warp; g < nb; g += (long long)gridDim.x * warps) {
     EncodeArgs a;
     long long bl;
     resolve(w, g, a, bl);
@@ -1110,17 +1111,18 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
   }
 }
 
-// Shared memory the warp kernel needs for `m` candidates, or 0 when it does
-// not fit (the thread-per-block kernel then handles the launch).
-size_t rand_smem_bytes(int m) {
-  const size_t bytes = rand_layout(m).bytes * kRandWarps;
+// Shared memory the warp kernel needs for `m` candidates and `warps` warps per
+// CTA, or 0 when it does not fit (the thread-per-block kernel then handles
+// the launch).
+size_t rand_smem_bytes(int m, int warps) {
+  const size_t bytes = rand_layout(m).bytes * warps;
   return bytes <= 200 * 1024 ? bytes : 0;
 }
 
 // Raises the kernel's dynamic shared memory limit only when a launch needs more
 // than any earlier one (the attribute persists), then launches.
 template <int DXT, int REFINE>
-cudaError_t launch_rand(const EncodeWork& a, int m, size_t smem, unsigned grid, cudaStream_t s) {
+cudaError_t launch_rand(const EncodeWork& a, int m, size_t smem, unsigned grid, int warps, cudaStream_t s) {
   static int limit = 48 * 1024;
   if (int(smem) > limit) {
     const cudaError_t e =
@@ -1128,35 +1130,45 @@ cudaError_t launch_rand(const EncodeWork& a, int m, size_t smem, unsigned grid, 
     if (e != cudaSuccess) return e;
     limit = int(smem);
   }
-  k_encode_rand<DXT, REFINE><<<grid, 32 * kRandWarps, smem, s>>>(a, m);
+  k_encode_rand<DXT, REFINE><<<grid, 32 * warps, smem, s>>>(a, m);
   return cudaGetLastError();
 }
 
+// The launch layout comes from the tuning table (encode_layout): threads per
+// CTA of the thread-per-block kernels, and warps per CTA and CTAs per SM of
+// the warp kernel's persistent grid.  Every layout encodes the same bytes.
 template <int DXT, bool NORMAL>
 cudaError_t launch_r(const EncodeWork& a, int refine, cudaStream_t s) {
   const long long nb = a.total;
   if (nb == 0) return cudaSuccess;
-  const int threads = kThreadsPerCta;
-  const unsigned grid = unsigned((nb + threads - 1) / threads);
   if (NORMAL && a.nrandom > 0) {
+    const EncodeLayout L = encode_layout(kMetric, DXT, refine, kLayoutRand);
+    const int warps = std::max(1, std::min(kRandWarps, L.rand_warps));
     const int m = 16 + a.nrandom;
-    const size_t smem = rand_smem_bytes(m);
+    const size_t smem = rand_smem_bytes(m, warps);
     if (smem > 0) {
       count_launches(1);
-      const unsigned rgrid = unsigned(std::min<long long>((nb + kRandWarps - 1) / kRandWarps, 152ll * 64));
+      const unsigned rgrid =
+          unsigned(std::min<long long>((nb + warps - 1) / warps, 152ll * std::max(1, L.rand_ctas_per_sm)));
       switch (refine) {
-        case RF_NEVER: return launch_rand<DXT, RF_NEVER>(a, m, smem, rgrid, s);
-        case RF_LOOP: return launch_rand<DXT, RF_LOOP>(a, m, smem, rgrid, s);
-        default: return launch_rand<DXT, RF_ALWAYS>(a, m, smem, rgrid, s);
+        case RF_NEVER: return launch_rand<DXT, RF_NEVER>(a, m, smem, rgrid, warps, s);
+        case RF_LOOP: return launch_rand<DXT, RF_LOOP>(a, m, smem, rgrid, warps, s);
+        default: return launch_rand<DXT, RF_ALWAYS>(a, m, smem, rgrid, warps, s);
       }
     }
   }
+  const int kind = NORMAL ? (a.nrandom > 0 ? kLayoutRand : kLayoutFull) : kLayoutQuick;
+  const EncodeLayout L = encode_layout(kMetric, DXT, refine, kind);
+  const int threads = std::max(32, std::min(kThreadsPerCta, L.threads & ~31));
+  const unsigned grid = unsigned((nb + threads - 1) / threads);
   if (NORMAL && a.nrandom <= 0) {
+    // the full-block kernel's shared columns are laid out for kThreadsPerCta
+    const unsigned grid16 = unsigned((nb + kThreadsPerCta - 1) / kThreadsPerCta);
     count_launches(1);
     switch (refine) {
-      case RF_NEVER: k_encode_full16<DXT, RF_NEVER><<<grid, threads, 0, s>>>(a); break;
-      case RF_LOOP: k_encode_full16<DXT, RF_LOOP><<<grid, threads, 0, s>>>(a); break;
-      default: k_encode_full16<DXT, RF_ALWAYS><<<grid, threads, 0, s>>>(a); break;
+      case RF_NEVER: k_encode_full16<DXT, RF_NEVER><<<grid16, kThreadsPerCta, 0, s>>>(a); break;
+      case RF_LOOP: k_encode_full16<DXT, RF_LOOP><<<grid16, kThreadsPerCta, 0, s>>>(a); break;
+      default: k_encode_full16<DXT, RF_ALWAYS><<<grid16, kThreadsPerCta, 0, s>>>(a); break;
     }
   }
   count_launches(1);

@@ -37,6 +37,17 @@ struct EncodeWork {
   EncodeArgs single;
 };
 
+// Launch layout of the encoder kernels for one mode (the autotuner's knobs;
+// no effect on the bytes).
+enum { kLayoutQuick = 0, kLayoutFull = 1, kLayoutRand = 2 };
+struct EncodeLayout {
+  int threads;           // threads per CTA of the thread-per-block kernels (32..128)
+  int rand_warps;        // warps per CTA of the random-candidate kernel (1..4)
+  int rand_ctas_per_sm;  // its persistent grid: CTAs per SM
+};
+EncodeLayout encode_layout(int metric, int dxt, int refine, int kind);
+void set_encode_layout(int metric, int dxt, int refine, int kind, EncodeLayout layout);
+
 cudaError_t launch_encode_m0(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
 cudaError_t launch_encode_m1(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);
 cudaError_t launch_encode_m2(const EncodeWork&, int dxt, bool normal, int refine, cudaStream_t);

@@ -372,3 +372,28 @@ def test_device_rand_stream_continues(lib, oracle):
         for _ in range(words):
             pyoracle.libc_rand()
         assert after == pyoracle.libc_rand()
+
+
+def test_launch_layouts_same_bytes(lib, oracle):
+    """Every launch layout the autotuner may pick encodes the same bytes, and
+    the autotuner itself leaves libc's rand() stream alone."""
+    rng = np.random.default_rng(5)
+    w, h = 200, 120
+    img = cases.image(rng, w, h, 4, 1)
+    for fmt, (metric, nr, refine) in ((0x83F3, (5, 24, 1)), (0x83F1, (3, -1, 2)), (0x83F2, (7, 0, 2))):
+        want = oracle.compress(4, w, h, img, fmt, 1, metric, nr, refine, seed=3)
+        opt = s2.options(1, metric, nr, refine)
+        layouts = ([(128, wp, cps) for wp in (1, 2, 4) for cps in (1, 8, 64)] if nr > 0
+                   else [(t, 4, 64) for t in (32, 64, 96, 128)])
+        for layout in layouts:
+            s2.set_layout(opt, fmt, *layout)
+            a = gpu_compress(4, w, h, img, fmt, 1, metric, nr, refine, seed=3)
+            assert np.array_equal(a, want), (hex(fmt), layout)
+        pyoracle.srand(9)
+        ms = s2.autotune(opt, fmt, 512, 256)
+        assert ms > 0
+        x = pyoracle.libc_rand()
+        pyoracle.srand(9)
+        assert x == pyoracle.libc_rand()
+        a = gpu_compress(4, w, h, img, fmt, 1, metric, nr, refine, seed=3)
+        assert np.array_equal(a, want), hex(fmt)
