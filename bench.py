@@ -387,6 +387,7 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
         for f in ((0x83F1, 0x83F2, 0x83F3) if wl["gen"] == "mips" else (wl["fmt"],)):
             s2.autotune(opt, f, 1024, 1024)
             layouts[FMT_NAMES[f]] = s2.get_layout(opt, f)
+    if wl["gen"] == "mips":
         tex = workloads.mip_textures(wl["seed"], count=wl["count"], lo=4, hi=2048)
         levels = [(t, lvl) for t in tex for lvl in t["levels"]]
     else:
