@@ -10,7 +10,7 @@
 //   v[t+m] = sum_i a_i v[t+i]  where  x^m = sum_i a_i x^i  mod  x^31 - x^28 - 1,
 // and a chunk of the stream starting m values ahead is reached with
 // O(log m) products of degree-30 polynomials.  Each GPU thread jumps to its
-// chunk this way and then runs the recurrence for kChunk values; the host
+// chunk this way and then runs the recurrence for its values; the host
 // jumps libc's own state ahead by the words consumed, so a later rand() in
 // the process continues exactly where the reference's encoder would have
 // left it.
@@ -36,7 +36,6 @@ namespace {
 
 constexpr int kDeg = 31, kSep = 3, kTypes = 5, kType3 = 3;
 constexpr int kPowers = 63;            // x^(2^k) mod f for k < 63
-constexpr int kChunk = kDeg * 128;     // values per thread (a multiple of 31)
 
 // Polynomials mod f(x) = x^31 - x^28 - 1 over Z/2^32, 31 coefficients.
 __host__ __device__ inline void poly_mulmod(const uint32_t* a, const uint32_t* b, uint32_t* out) {
@@ -90,46 +89,118 @@ __host__ __device__ inline void poly_pow(const uint32_t (*T)[kDeg], unsigned lon
     }
 }
 
-// One thread per chunk of kChunk values: jump, then run the recurrence.
-__global__ void __launch_bounds__(128) k_rand_fill(const RandWindow* __restrict__ win,
-                                                    const PowerTable* __restrict__ pw, uint32_t* __restrict__ out,
-                                                    long long n) {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long start = c * kChunk;
-  if (start >= n) return;
+// Kernel layout: a CTA of kFillThreads threads covers kSuper consecutive
+// values; thread t owns the kSub values at t * kSub.  Warp 0 computes the
+// CTA's jump x^(CTA start) cooperatively (lane k owns coefficients k and
+// k + 31 of each product); every thread then multiplies by its own offset's
+// power, taken from a table of x^(t * kSub), forms its 31-value window and
+// runs the recurrence.  Values go out through shared memory, one 31-value
+// pass at a time, so that a warp's stores cover whole runs of consecutive
+// words.
+constexpr int kFillThreads = 128;
+constexpr int kPasses = 8;
+constexpr int kSub = kDeg * kPasses;           // 248 values per thread
+constexpr int kSuper = kSub * kFillThreads;    // 31744 values per CTA
+
+struct OffsetTable {
+  uint32_t t[kFillThreads][kDeg];  // x^(t * kSub) mod f
+};
+
+// out = a * b mod f by one warp; a, b, out in shared memory (out may alias a).
+__device__ void warp_mulmod(const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* tmp, int lane) {
+  // tmp[0..60] = the product's coefficients
+  for (int k = lane; k < 2 * kDeg - 1; k += 32) {
+    uint32_t s = 0;
+    const int lo = k < kDeg ? 0 : k - (kDeg - 1), hi = k < kDeg ? k : kDeg - 1;
+    for (int i = lo; i <= hi; ++i) s += a[i] * b[k - i];
+    tmp[k] = s;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    // the reduction mod f in registers
+    uint32_t c[2 * kDeg - 1];
+#pragma unroll
+    for (int k = 0; k < 2 * kDeg - 1; ++k) c[k] = tmp[k];
+#pragma unroll
+    for (int k = 2 * kDeg - 2; k >= kDeg; --k) {
+      c[k - 3] += c[k];
+      c[k - kDeg] += c[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kDeg; ++k) out[k] = c[k];
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kFillThreads) k_rand_fill(const RandWindow* __restrict__ win,
+                                                             const PowerTable* __restrict__ pw,
+                                                             const OffsetTable* __restrict__ offs,
+                                                             uint32_t* __restrict__ out, long long n) {
+  __shared__ uint32_t s_a[kDeg], s_b[kDeg], s_tmp[2 * kDeg];
+  __shared__ uint32_t s_ext[61];
+  __shared__ uint32_t s_pass[kFillThreads / 32][32][kDeg + 2];  // odd row stride: no bank conflicts
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const long long cta0 = (long long)blockIdx.x * kSuper;
+  if (t < 61) s_ext[t] = __ldg(win->ext + t);
+  if (warp == 0) {
+    // x^cta0 by square-and-multiply over the table of x^(2^k)
+    if (lane < kDeg) s_a[lane] = lane == 0 ? 1u : 0u;
+    __syncwarp();
+    unsigned long long m = (unsigned long long)cta0;
+    for (int k = 0; m; ++k, m >>= 1) {
+      if (!(m & 1)) continue;
+      if (lane < kDeg) s_b[lane] = __ldg(&pw->t[k][lane]);
+      __syncwarp();
+      warp_mulmod(s_a, s_b, s_a, s_tmp, lane);
+    }
+  }
+  __syncthreads();
+  const long long start = cta0 + (long long)t * kSub;
+  // a = x^start = x^cta0 * x^(t * kSub)
   uint32_t a[kDeg];
-  poly_pow(pw->t, (unsigned long long)start, a);
+  {
+    uint32_t x0[kDeg], x1[kDeg];
+#pragma unroll
+    for (int i = 0; i < kDeg; ++i) {
+      x0[i] = s_a[i];
+      x1[i] = __ldg(&offs->t[t][i]);
+    }
+    poly_mulmod(x0, x1, a);
+  }
   // w[j] = v[start - 31 + j] = sum_i a_i v[-31 + j + i]
   uint32_t w[kDeg];
+  {
+    uint32_t e[61];
 #pragma unroll
-  for (int j = 0; j < kDeg; ++j) {
-    uint32_t s = 0;
-#pragma unroll 1
-    for (int i = 0; i < kDeg; ++i) s += a[i] * __ldg(win->ext + j + i);
-    w[j] = s;
+    for (int k = 0; k < 61; ++k) e[k] = s_ext[k];
+#pragma unroll
+    for (int j = 0; j < kDeg; ++j) {
+      uint32_t s = 0;
+#pragma unroll
+      for (int i = 0; i < kDeg; ++i) s += a[i] * e[j + i];
+      w[j] = s;
+    }
   }
-  const long long end = start + kChunk < n ? start + kChunk : n;
-  uint32_t* o = out + start;
-  long long t = start;
-  while (t + kDeg <= end) {
+  uint32_t(*pass)[kDeg + 2] = s_pass[warp];
+  for (int p = 0; p < kPasses; ++p) {
 #pragma unroll
     for (int j = 0; j < kDeg; ++j) {
       w[j] += w[(j + kDeg - kSep) % kDeg];
-      o[j] = w[j] >> 1;
+      pass[lane][j] = w[j] >> 1;
     }
-    o += kDeg;
-    t += kDeg;
-  }
-#pragma unroll
-  for (int j = 0; j < kDeg; ++j) {
-    if (t + j >= end) break;
-    w[j] += w[(j + kDeg - kSep) % kDeg];
-    o[j] = w[j] >> 1;
+    __syncwarp();
+    // the warp writes each lane's 31 values as one run (lanes 0..30 cover a run)
+    for (int r = 0; r < 32; ++r) {
+      const long long base = cta0 + (long long)(warp * 32 + r) * kSub + (long long)p * kDeg;
+      if (lane < kDeg && base + lane < n) out[base + lane] = pass[r][lane];
+    }
+    __syncwarp();
   }
 }
 
 std::mutex g_mu;
 PowerTable* g_dev_powers = nullptr;  // one copy (single-device library)
+OffsetTable* g_dev_offsets = nullptr;
 
 }  // namespace
 
@@ -179,12 +250,22 @@ bool rand_usable() {
 cudaError_t rand_prepare() {
   std::lock_guard<std::mutex> lock(g_mu);
   if (g_dev_powers) return cudaSuccess;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&g_dev_powers), sizeof(PowerTable));
-  if (e == cudaSuccess) e = cudaMemcpy(g_dev_powers, &host_powers(), sizeof(PowerTable), cudaMemcpyHostToDevice);
+  OffsetTable* offs = new OffsetTable();
+  for (int t = 0; t < kFillThreads; ++t) poly_pow(host_powers().t, (unsigned long long)t * kSub, offs->t[t]);
+  PowerTable* dp = nullptr;
+  OffsetTable* doffs = nullptr;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&dp), sizeof(PowerTable));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&doffs), sizeof(OffsetTable));
+  if (e == cudaSuccess) e = cudaMemcpy(dp, &host_powers(), sizeof(PowerTable), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(doffs, offs, sizeof(OffsetTable), cudaMemcpyHostToDevice);
+  delete offs;
   if (e != cudaSuccess) {
-    cudaFree(g_dev_powers);
-    g_dev_powers = nullptr;
+    cudaFree(dp);
+    cudaFree(doffs);
+    return e;
   }
+  g_dev_powers = dp;
+  g_dev_offsets = doffs;
   return e;
 }
 
@@ -192,9 +273,9 @@ cudaError_t rand_fill(const RandWindow* d_w, uint32_t* d_out, long long n, cudaS
   if (n <= 0) return cudaSuccess;
   const cudaError_t e = rand_prepare();
   if (e != cudaSuccess) return e;
-  const long long chunks = (n + kChunk - 1) / kChunk;
+  const long long ctas = (n + kSuper - 1) / kSuper;
   count_launches(1);
-  k_rand_fill<<<unsigned((chunks + 127) / 128), 128, 0, s>>>(d_w, g_dev_powers, d_out, n);
+  k_rand_fill<<<unsigned(ctas), kFillThreads, 0, s>>>(d_w, g_dev_powers, g_dev_offsets, d_out, n);
   return cudaGetLastError();
 }
 
