@@ -622,8 +622,13 @@ def run_tool_workload(args, wl_name: str, wl: dict) -> None:
             cpu = {"value": rows * w / dt, "unit": "texels/s", "cores": 1, "kind": "port",
                    "sample": f"the first {rows} rows ({rows * w} texels), single thread ({dt:.2f} s)"}
         kernel = "k_decode" if wl["tool"] == "decode" else "k_from_s3tc"
+        traffic = None
+        try:
+            traffic = json.loads((ROOT / "profiles" / "traffic.json").read_text()).get(wl_name, {}).get(kernel)
+        except Exception:
+            pass
         roofline = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                    "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_launch": alg}
+                    "frac": achieved / hbm, "traffic": traffic, "algorithmic_bytes_per_launch": alg}
         ms = 1000 * t / args.steps
     else:
         img = workloads.plain_rgba(wl["seed"], w, h)
