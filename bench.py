@@ -59,6 +59,9 @@ WORKLOADS = {
     # mixed DXT1/DXT3/DXT5, RGB8/RGBA8: one batched graph launch per step
     "mip_chains_256_wavg_rand64_always": dict(
         w=0, h=0, sc=0, fmt=0, dither=1, metric=5, nrandom=64, refine=1, gen="mips", seed=3, count=256),
+    # the first 64 of those textures (a size that ncu captures whole)
+    "mip_chains_64_wavg_rand64_always": dict(
+        w=0, h=0, sc=0, fmt=0, dither=1, metric=5, nrandom=64, refine=1, gen="mips", seed=3, count=64),
     # 64 RGB8 normal maps of 2048x2048 (16 distinct maps, each used four
     # times) in one batched graph launch
     "normal_maps_64x2048_dxt1_normalmap_rand64_loop": dict(
