@@ -389,6 +389,18 @@ __device__ __forceinline__ void load_block(const uint32_t* __restrict__ t565, in
   bt.w = min(4, width - bx * 4);
   bt.h = min(4, height - by * 4);
   const uint32_t* p = t565 + size_t(by) * 4 * width + size_t(bx) * 4;
+  if (bt.w == 4 && bt.h == 4 && ((reinterpret_cast<uintptr_t>(p) | (size_t(width) * 4)) & 15) == 0) {
+    // whole block, rows 16-byte aligned: one vector load per row
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(p + size_t(y) * width));
+      bt.px[y * 4 + 0] = v.x;
+      bt.px[y * 4 + 1] = v.y;
+      bt.px[y * 4 + 2] = v.z;
+      bt.px[y * 4 + 3] = v.w;
+    }
+    return;
+  }
 #pragma unroll
   for (int y = 0; y < 4; ++y)
 #pragma unroll

@@ -83,8 +83,19 @@ __device__ __forceinline__ int32_t nm_dist(NUnit a, NUnit b) {
 // Each metric is evaluated on a per-colour "prepared" form computed once per
 // colour: the squared components for SRGB, (Y, U, V) with the square-rooted
 // luma for SRGB_MIXED, the unit vector for NORMALMAP, the plain components
-// otherwise.  pdist(prep(a), prep(b)) equals the reference's dist(a, b)
-// operation for operation.
+// for RGB and YUV.  pdist(prep(a), prep(b)) equals the reference's dist(a, b)
+// exactly.
+//
+// The AVG family is a weighted sum of squares with weights 1 or 4 = 2^2, so
+// its prepared form packs the components times their weight's square root as
+// bytes (at most 2 * 63 = 126): byte-wise differences then fit signed bytes
+// and one dp4a sums their squares.  The differences come from one 32-bit
+// subtraction that cannot borrow across bytes: (a | 0x80 per byte) - b keeps
+// every byte in [2, 254], and flipping bit 7 back gives the signed difference.
+struct Pk {
+  uint32_t v;  // byte 0: red, 1: green, 2: blue, each times 1 or 2; byte 3: 0
+};
+
 template <int METRIC>
 struct PrepT {
   using T = C3;
@@ -93,6 +104,23 @@ template <>
 struct PrepT<CD_NORMALMAP> {
   using T = NUnit;
 };
+template <>
+struct PrepT<CD_AVG> {
+  using T = Pk;
+};
+template <>
+struct PrepT<CD_WAVG> {
+  using T = Pk;
+};
+template <>
+struct PrepT<CD_W0AVG> {
+  using T = Pk;
+};
+
+__device__ __forceinline__ int32_t pk_dist(Pk a, Pk b) {
+  const uint32_t x = ((a.v | 0x80808080u) - b.v) ^ 0x80808080u;
+  return __dp4a(int(x), int(x), 0);
+}
 
 template <int METRIC>
 __device__ __forceinline__ typename PrepT<METRIC>::T prep(C3 c) {
@@ -103,6 +131,12 @@ __device__ __forceinline__ typename PrepT<METRIC>::T prep(C3 c) {
     return C3{y, c.r * 191 - y, c.b * 191 - y};
   } else if constexpr (METRIC == CD_NORMALMAP) {
     return nm_unit(c);
+  } else if constexpr (METRIC == CD_AVG) {  // 4 dr^2 + dg^2 + 4 db^2
+    return Pk{uint32_t(2 * c.r) | (uint32_t(c.g) << 8) | (uint32_t(2 * c.b) << 16)};
+  } else if constexpr (METRIC == CD_WAVG) {  // 4 dr^2 + 4 dg^2 + db^2
+    return Pk{uint32_t(2 * c.r) | (uint32_t(2 * c.g) << 8) | (uint32_t(c.b) << 16)};
+  } else if constexpr (METRIC == CD_W0AVG) {  // dr^2 + dg^2 + db^2
+    return Pk{uint32_t(c.r) | (uint32_t(c.g) << 8) | (uint32_t(c.b) << 16)};
   } else {
     return c;
   }
@@ -112,15 +146,8 @@ template <int METRIC>
 __device__ __forceinline__ int32_t pdist(const typename PrepT<METRIC>::T& a, const typename PrepT<METRIC>::T& b) {
   if constexpr (METRIC == CD_NORMALMAP) {
     return nm_dist(a, b);
-  } else if constexpr (METRIC == CD_AVG) {
-    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
-    return ((dr * dr) << 2) + dg * dg + ((db * db) << 2);
-  } else if constexpr (METRIC == CD_W0AVG) {
-    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
-    return dr * dr + dg * dg + db * db;
-  } else if constexpr (METRIC == CD_WAVG) {
-    int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
-    return ((dr * dr) << 2) + ((dg * dg) << 2) + db * db;
+  } else if constexpr (METRIC == CD_AVG || METRIC == CD_W0AVG || METRIC == CD_WAVG) {
+    return pk_dist(a, b);
   } else if constexpr (METRIC == CD_YUV || METRIC == CD_RGB) {
     int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
     int y = METRIC == CD_YUV ? dr * 60 + dg * 59 + db * 22 : dr * 42 + dg * 72 + db * 14;
