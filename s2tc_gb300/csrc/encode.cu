@@ -746,6 +746,10 @@ __device__ __forceinline__ uint32_t pair_sq_sum16(const uint4* a, const uint4* b
   return s;
 }
 
+#ifndef S2TC_PAIR_UNROLL
+#define S2TC_PAIR_UNROLL 4
+#endif
+constexpr int kPairUnroll = S2TC_PAIR_UNROLL;  // partner rows unrolled per tile row
 // Walks every pair i < j < mm: 8-row tiles (I, J), I <= J, four groups of
 // eight lanes per warp, each group one tile at a time; lane r of a group owns
 // row I*8 + r and visits the tile's eight partner rows.  `load(k, row)` reads
@@ -767,6 +771,7 @@ __device__ __forceinline__ void tiled_pairs(int mm, int lane, Load load, Sum sum
     const int i = I * 8 + r;
     RowT ri;
     load(min(i, mm - 1), ri);
+#pragma unroll kPairUnroll
     for (int jj = 0; jj < 8; ++jj) {
       const int j = J * 8 + jj;
       RowT rj;
