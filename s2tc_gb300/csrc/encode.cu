@@ -52,7 +52,8 @@ struct Scratch16 {
 
 // Pick the pair the reference keeps: pairs in (i, j) lexicographic order,
 // taken when `bestsum < 0 || sum < bestsum` (s2tc_algorithm.cpp:404-409).
-__device__ __forceinline__ void pick_pair(const int32_t* S, int& besti, int& bestj) {
+// Only pairs of inputs in `mask` (bit k: input k takes part) are candidates.
+__device__ __forceinline__ void pick_pair(const int32_t* S, uint32_t mask, int& besti, int& bestj) {
   int32_t bestsum = -1;
   besti = 0;
   bestj = 1;
@@ -61,7 +62,8 @@ __device__ __forceinline__ void pick_pair(const int32_t* S, int& besti, int& bes
   for (int i = 0; i < 16; ++i)
 #pragma unroll
     for (int j = i + 1; j < 16; ++j, ++p) {
-      const bool take = bestsum < 0 || S[p] < bestsum;
+      const bool ok = ((mask >> i) & (mask >> j) & 1u) != 0;
+      const bool take = ok && (bestsum < 0 || S[p] < bestsum);
       bestsum = take ? S[p] : bestsum;
       besti = take ? i : besti;
       bestj = take ? j : bestj;
@@ -71,7 +73,7 @@ __device__ __forceinline__ void pick_pair(const int32_t* S, int& besti, int& bes
 // reduce_colors_inplace (s2tc_algorithm.cpp:363-414) for n = m = 16.  Between
 // two inputs the reference evaluates dist(c[lo], c[hi]) once and uses it both
 // ways; d(k, k) = 0.
-__device__ __forceinline__ void reduce16_rgb(const P* tp, Scratch16& sc, int& besti, int& bestj) {
+__device__ __forceinline__ void reduce16_rgb(const P* tp, uint32_t mask, Scratch16& sc, int& besti, int& bestj) {
   const int t = threadIdx.x;
   P pin[16];
 #pragma unroll
@@ -84,6 +86,7 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, Scratch16& sc, int& be
   for (int p = 0; p < 120; ++p) S[p] = 0;
 #pragma unroll 1
   for (int k = 0; k < 16; ++k) {
+    if (!((mask >> k) & 1u)) continue;  // a transparent DXT1 texel is no input
     const P pk = sc.pin[k][t];
     int32_t col[16];
 #pragma unroll
@@ -95,7 +98,7 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, Scratch16& sc, int& be
 #pragma unroll
       for (int j = i + 1; j < 16; ++j, ++p) S[p] = wadd(S[p], min(col[i], col[j]));
   }
-  pick_pair(S, besti, bestj);
+  pick_pair(S, mask, besti, bestj);
 }
 
 // reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) for n = m = 16
@@ -127,7 +130,7 @@ __device__ __forceinline__ void reduce16_alpha(const int* ain, Scratch16& sc, in
         S[p] += v * v;
       }
   }
-  pick_pair(S, besti, bestj);
+  pick_pair(S, 0xFFFFu, besti, bestj);
 }
 
 // ------------------------------------------------------------------------
@@ -243,14 +246,24 @@ struct EncodedBlock {
 // A block takes the full-block search when it has 16 inputs: all 16 texels
 // inside the image and, for DXT1, none of them transparent (the reference
 // leaves alpha-0 texels out of the candidate list, :947-949).
+// Inputs of a whole block in x-outer, y-inner order (bit k: input k): DXT1
+// leaves transparent texels out (s2tc_algorithm.cpp:940-951).
 template <int DXT>
-__device__ __forceinline__ bool is_full(const BlockTexels& bt) {
-  bool full = bt.w == 4 && bt.h == 4;
+__device__ __forceinline__ uint32_t input_mask(const BlockTexels& bt) {
+  uint32_t m = 0xFFFFu;
   if (DXT == DXT1) {
 #pragma unroll
-    for (int i = 0; i < 16; ++i) full = full && (bt.px[i] >> 24) != 0;
+    for (int k = 0; k < 16; ++k)
+      if ((bt.px[in_slot(k)] >> 24) == 0) m &= ~(1u << k);
   }
-  return full;
+  return m;
+}
+
+// Blocks of the register-resident all-texels search: 4x4 blocks with at
+// least two inputs (fewer take the general search's special cases).
+template <int DXT>
+__device__ __forceinline__ bool is_full(const BlockTexels& bt) {
+  return bt.w == 4 && bt.h == 4 && (DXT != DXT1 || __popc(input_mask<DXT>(bt)) >= 2);
 }
 
 // s2tc_encode_block<> (s2tc_algorithm.cpp:872-1108) for one block.
@@ -296,7 +309,7 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
   } else {
     if constexpr (FULL16) {
       int bi, bj;
-      reduce16_rgb(tp, sc, bi, bj);
+      reduce16_rgb(tp, input_mask<DXT>(bt), sc, bi, bj);
       c0 = texel_c3(bt.px[(bi & 3) * 4 + (bi >> 2)]);
       c1 = texel_c3(bt.px[(bj & 3) * 4 + (bj >> 2)]);
       if (DXT == DXT5) {
