@@ -157,6 +157,14 @@ int s2tc_server_create(s2tc_server **out, long long budget_bytes);
 int s2tc_server_submit(s2tc_server *server, const void *src, int srccomps, int width, int height,
 		       unsigned int format, const s2tc_options *opt, void *dst, long long dst_pitch,
 		       long long *id);
+/* The same for device-resident requests: `d_src` and `d_dst` are device
+ * pointers; nothing is copied, the pool holds only the request's texel words
+ * (and random-candidate words), and the blocks are written straight into
+ * `d_dst` (block rows `dst_pitch` bytes apart, 0 = packed).  The input must
+ * stay valid and the output untouched until s2tc_server_wait returns. */
+int s2tc_server_submit_device(s2tc_server *server, const void *d_src, int srccomps, int width, int height,
+			      unsigned int format, const s2tc_options *opt, void *d_dst, long long dst_pitch,
+			      long long *id);
 /* Block until request `id` is done; its latency (submission to completion)
  * in milliseconds.  Each id can be waited for once. */
 int s2tc_server_wait(s2tc_server *server, long long id, double *latency_ms);

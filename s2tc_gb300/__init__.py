@@ -130,6 +130,9 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_server_submit.argtypes = [vp, vp, c_int, c_int, c_int, c_uint, ctypes.POINTER(Options), vp, c_ll,
                                        ctypes.POINTER(c_ll)]
     lib.s2tc_server_submit.restype = c_int
+    lib.s2tc_server_submit_device.argtypes = [vp, vp, c_int, c_int, c_int, c_uint, ctypes.POINTER(Options), vp,
+                                              c_ll, ctypes.POINTER(c_ll)]
+    lib.s2tc_server_submit_device.restype = c_int
     lib.s2tc_server_wait.argtypes = [vp, c_ll, ctypes.POINTER(ctypes.c_double)]
     lib.s2tc_server_wait.restype = c_int
     lib.s2tc_server_stats.argtypes = [vp, ctypes.POINTER(c_ll), ctypes.POINTER(c_ll), ctypes.POINTER(c_int),
@@ -173,7 +176,7 @@ EXPORTED_SYMBOLS = (
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
     "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
     "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
-    "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit",
+    "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit", "s2tc_server_submit_device",
     "s2tc_server_wait", "s2tc_server_stats", "s2tc_server_destroy",
     "s2tc_gpu_encode_blocks", "s2tc_autotune", "s2tc_encode_layout_set", "s2tc_encode_layout_get", "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
     "s2tc_gpu_from_s3tc", "s2tc_from_s3tc_dds",
@@ -407,6 +410,16 @@ class Server:
         if st != S2TC_OK:
             raise S2tcError(f"s2tc_server_submit failed ({st})")
         self._keep[rid.value] = (src, dst)
+        return rid.value
+
+    def submit_device(self, d_src, srccomps: int, width: int, height: int, fmt: int, opt: Options, d_dst,
+                      dst_pitch: int = 0) -> int:
+        rid = ctypes.c_longlong()
+        st = load().s2tc_server_submit_device(self.handle, _addr(d_src), srccomps, width, height, fmt,
+                                              ctypes.byref(opt), _addr(d_dst), dst_pitch, ctypes.byref(rid))
+        if st != S2TC_OK:
+            raise S2tcError(f"s2tc_server_submit_device failed ({st})")
+        self._keep[rid.value] = (d_src, d_dst)
         return rid.value
 
     def wait(self, rid: int) -> float:

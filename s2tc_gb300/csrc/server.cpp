@@ -116,6 +116,7 @@ struct Req {
   s2tc_options opt{};
   uint8_t* hdst = nullptr;
   long long dpitch = 0;
+  bool device_io = false;      // hsrc / hdst are device pointers: no copies, no pool space
   long long npx = 0, bw = 0, bh = 0;
   size_t in_bytes = 0, tex_bytes = 0, out_bytes = 0, rand_bytes = 0, total = 0;
   std::vector<unsigned> rand;  // replayed rand() words (random-candidate mode, host loop)
@@ -176,7 +177,8 @@ int launch_round(s2tc_server* sv, Slot& sl) {
   if (cudaMemsetAsync(sl.d_err, 0, sizeof(int), s) != cudaSuccess) return S2TC_ERR_CUDA;
   // uploads
   for (auto& r : rs) {
-    if (cudaMemcpyAsync(base + r->off, r->hsrc, r->in_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
+    if (!r->device_io &&
+        cudaMemcpyAsync(base + r->off, r->hsrc, r->in_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
       return S2TC_ERR_CUDA;
     if (r->rand_bytes && !r->dev_rand &&
         cudaMemcpyAsync(base + r->off + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign) +
@@ -224,10 +226,11 @@ int launch_round(s2tc_server* sv, Slot& sl) {
     for (int i = 0; i < n; ++i) {
       Req* r = v[i];
       unsigned char* p = base + r->off;
-      const uint8_t* din = p;
+      const uint8_t* din = r->device_io ? r->hsrc : p;
       uint32_t* tex = reinterpret_cast<uint32_t*>(p + align_up(r->in_bytes, kAlign));
-      uint8_t* dout = p + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign);
-      const unsigned* drand = reinterpret_cast<const unsigned*>(dout + align_up(r->out_bytes, kAlign));
+      uint8_t* pout = p + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign);
+      uint8_t* dout = r->device_io ? r->hdst : pout;
+      const unsigned* drand = reinterpret_cast<const unsigned*>(pout + align_up(r->out_bytes, kAlign));
       di[i] = DitherItem{din, r->w, r->h, r->sc, r->dxt == DXT1 ? 1 : r->dxt == DXT3 ? 4 : 8, tex};
       to[i] = tiles;
       tiles += (r->npx + tile_tex - 1) / tile_tex;
@@ -240,8 +243,9 @@ int launch_round(s2tc_server* sv, Slot& sl) {
       a.by0 = 0;
       a.nby = int(r->bh);
       a.dst = dout;
-      a.pitch = r->bw * (r->dxt == DXT1 ? 8 : 16);
-      a.aligned = 1;
+      const int bsz = r->dxt == DXT1 ? 8 : 16;
+      a.pitch = r->device_io ? r->dpitch : r->bw * bsz;
+      a.aligned = ((reinterpret_cast<uintptr_t>(dout) % bsz) == 0 && (a.pitch % bsz) == 0) ? 1 : 0;
       a.nrandom = r->opt.nrandom;
       a.rnd = r->rand_bytes ? drand : nullptr;
       a.prev_a1_first = -1;
@@ -320,6 +324,7 @@ int launch_round(s2tc_server* sv, Slot& sl) {
   if (cudaMemcpyAsync(sl.h_err, sl.d_err, sizeof(int), cudaMemcpyDeviceToHost, sv->copy_out) != cudaSuccess)
     return S2TC_ERR_CUDA;
   for (auto& r : rs) {
+    if (r->device_io) continue;  // the encoder wrote the caller's device buffer
     const size_t row = size_t(r->bw) * (r->dxt == DXT1 ? 8 : 16);
     const uint8_t* dout = base + r->off + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign);
     if (cudaMemcpy2DAsync(r->hdst, size_t(r->dpitch), dout, row, row, size_t(r->bh), cudaMemcpyDeviceToHost,
@@ -453,8 +458,8 @@ int s2tc_server_create(s2tc_server** out, long long budget_bytes) {
   return S2TC_OK;
 }
 
-int s2tc_server_submit(s2tc_server* sv, const void* src, int srccomps, int width, int height, unsigned int format,
-                       const s2tc_options* opt, void* dst, long long dst_pitch, long long* id) {
+static int server_submit(s2tc_server* sv, const void* src, int srccomps, int width, int height, unsigned int format,
+                         const s2tc_options* opt, void* dst, long long dst_pitch, long long* id, bool device_io) {
   using namespace s2tc;
   if (!sv || !src || !dst || !opt || !id || width <= 0 || height <= 0) return S2TC_ERR_ARGUMENT;
   const int dxt = fmt_dxt(format);
@@ -473,9 +478,10 @@ int s2tc_server_submit(s2tc_server* sv, const void* src, int srccomps, int width
   const long long row = r->bw * (dxt == s2tc::DXT1 ? 8 : 16);
   r->dpitch = dst_pitch > 0 ? dst_pitch : row;
   if (r->dpitch < row) return S2TC_ERR_ARGUMENT;
-  r->in_bytes = size_t(r->npx) * r->sc;
+  r->device_io = device_io;
+  r->in_bytes = device_io ? 0 : size_t(r->npx) * r->sc;
   r->tex_bytes = size_t(r->npx) * 4;
-  r->out_bytes = size_t(row) * r->bh;
+  r->out_bytes = device_io ? 0 : size_t(row) * r->bh;
   const bool normal = r->opt.nrandom >= 0 || r->opt.metric == CD_NORMALMAP;
   if (normal && r->opt.nrandom > 0) {
     // libc rand() drawn now, in submission order, as tx_compress_dxtn would
@@ -500,6 +506,17 @@ int s2tc_server_submit(s2tc_server* sv, const void* src, int srccomps, int width
   *id = r->id;
   sv->cv_submit.notify_one();
   return S2TC_OK;
+}
+
+int s2tc_server_submit(s2tc_server* sv, const void* src, int srccomps, int width, int height, unsigned int format,
+                       const s2tc_options* opt, void* dst, long long dst_pitch, long long* id) {
+  return server_submit(sv, src, srccomps, width, height, format, opt, dst, dst_pitch, id, false);
+}
+
+int s2tc_server_submit_device(s2tc_server* sv, const void* d_src, int srccomps, int width, int height,
+                              unsigned int format, const s2tc_options* opt, void* d_dst, long long dst_pitch,
+                              long long* id) {
+  return server_submit(sv, d_src, srccomps, width, height, format, opt, d_dst, dst_pitch, id, true);
 }
 
 int s2tc_server_wait(s2tc_server* sv, long long id, double* latency_ms) {

@@ -130,3 +130,32 @@ def test_server_threads_and_rounds(lib):
     s2.set_env(1, s2.SRGB_MIXED, 0, 2)
     for img, src, dst in bufs:
         assert np.array_equal(dst.numpy(), s2.tx_compress_dxtn(4, w, h, img, 0x83F3))
+
+
+def test_server_device_resident_requests(lib):
+    """Device-resident requests (no copies, blocks written in place, padded
+    rows) mixed with host requests give tx_compress_dxtn's bytes."""
+    torch = pytest.importorskip("torch")
+    srv = s2.Server(256 << 20)
+    opt = s2.options(1, s2.SRGB_MIXED, 0, 2)
+    jobs = []
+    for k, (w, h, fmt) in enumerate([(100, 60, 0x83F3), (257, 129, 0x83F1), (64, 64, 0x83F2), (33, 5, 0x83F3)]):
+        img = workloads.value_noise_rgba(70 + k, w, h).reshape(-1)
+        row = ((w + 3) // 4) * (8 if fmt == 0x83F1 else 16)
+        pitch = row + 32
+        d_src = torch.from_numpy(img).cuda()
+        d_dst = torch.zeros(pitch * ((h + 3) // 4), dtype=torch.uint8, device="cuda")
+        h_dst = torch.zeros(s2.compressed_size(w, h, fmt), dtype=torch.uint8).pin_memory()
+        a = srv.submit_device(d_src, 4, w, h, fmt, opt, d_dst, pitch)
+        b = srv.submit(torch.from_numpy(img).pin_memory(), 4, w, h, fmt, opt, h_dst)
+        jobs.append((img, w, h, fmt, row, pitch, d_dst, h_dst, a, b))
+    for j in jobs:
+        srv.wait(j[8])
+        srv.wait(j[9])
+    srv.close()
+    s2.set_env(1, s2.SRGB_MIXED, 0, 2)
+    for img, w, h, fmt, row, pitch, d_dst, h_dst, _, _ in jobs:
+        want = s2.tx_compress_dxtn(4, w, h, img, fmt)
+        got = d_dst.cpu().numpy().reshape(-1, pitch)[:, :row].reshape(-1)
+        assert np.array_equal(got, want), (w, h, hex(fmt))
+        assert np.array_equal(h_dst.numpy(), want), (w, h, hex(fmt))
