@@ -303,7 +303,71 @@ struct TileSmem {
   uint32_t wagg[kWarps][kRecWords];  // warps' inclusive records
   uint32_t wstart[kWarps];           // warps' start states
   uint32_t carry;
+  alignas(8) unsigned long long mbar;  // completion of the tile's bulk copy
 };
+
+// ------------------------------------------------ bulk copy (TMA) of a tile
+// A whole RGBA8 tile is contiguous in global memory (kTile * 4 bytes): one
+// thread starts bulk copies of it into shared memory (cp.async.bulk, the TMA
+// unit's non-tensor form) that signal an mbarrier with their byte count, and
+// every thread waits on that barrier.  Both addresses must be 16-byte aligned
+// and each size a multiple of 16; callers check.  The waits are bounded: on
+// timeout the error flag is set and the tile is loaded with ordinary loads.
+constexpr int kBulkChunk = 16384;  // bytes per bulk copy
+constexpr int kBulkSpins = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Thread 0 initialises the barrier; call before a __syncthreads.
+__device__ __forceinline__ void bulk_init(TileSmem& sm) {
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sm.mbar)) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+}
+
+// A second bounded wait for the barrier's phase (after a timeout).
+__device__ __forceinline__ void bulk_load_wait(TileSmem& sm) {
+  const uint32_t mbar = smem_u32(&sm.mbar);
+  int spins = 0;
+  while (!mbar_try_wait(mbar, 0) && ++spins < kBulkSpins) {
+  }
+}
+
+// Copies `bytes` (a multiple of 16) from `src` into sm.px; every thread
+// returns once the data is in shared memory.  Returns false on timeout.
+__device__ bool bulk_load(TileSmem& sm, const uint8_t* src, uint32_t bytes) {
+  const uint32_t mbar = smem_u32(&sm.mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+    const uint32_t dst = smem_u32(sm.px);
+    for (uint32_t off = 0; off < bytes; off += kBulkChunk) {
+      const uint32_t n = bytes - off < uint32_t(kBulkChunk) ? bytes - off : uint32_t(kBulkChunk);
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst + off),
+          "l"(src + off), "r"(n), "r"(mbar)
+          : "memory");
+    }
+  }
+  int spins = 0;
+  while (!mbar_try_wait(mbar, 0) && ++spins < kBulkSpins) {
+  }
+  return spins < kBulkSpins;
+}
 
 // Texels [p0, p0 + n) of `it` into px[0, n) as RGBA words (alpha 0 for RGB).
 __device__ __forceinline__ void load_tile(const DitherItem& it, long long p0, int n, uint32_t* px) {
@@ -562,6 +626,7 @@ __global__ void __launch_bounds__(kThreads, S2TC_DITHER_MINBLOCKS) k_dither_simp
   if (t < 64) sm.tab2[t] = swar_table_word<2>(t);
   if (t < 16) sm.tab4[t] = swar4_table_word(t);
   if (t == 0) s_ticket = atomicAdd(w.ticket, 1u);
+  bulk_init(sm);
   __syncthreads();
   const long long g = s_ticket;
   if (g >= w.total_tiles) return;
@@ -572,7 +637,17 @@ __global__ void __launch_bounds__(kThreads, S2TC_DITHER_MINBLOCKS) k_dither_simp
   const long long npx = (long long)it.width * it.height;
   const long long p0 = lt * kTile;
   const int n = int(min((long long)kTile, npx - p0));
-  load_tile(it, p0, n, sm.px);
+  const uint8_t* tsrc = it.src + p0 * 4;
+  if (it.srccomps == 4 && n == kTile && (reinterpret_cast<uintptr_t>(tsrc) & 15) == 0) {
+    if (!bulk_load(sm, tsrc, uint32_t(kTile) * 4u)) {
+      atomicExch(w.error, 1);
+      // give the copy another bounded wait before the buffer is reused
+      bulk_load_wait(sm);
+      load_tile(it, p0, n, sm.px);
+    }
+  } else {
+    load_tile(it, p0, n, sm.px);
+  }
   __syncthreads();
   if (it.srccomps == 3) simple_tile<0>(it, lt, g, n, w, sm);
   else if (it.alphabits == 1) simple_tile<1>(it, lt, g, n, w, sm);
