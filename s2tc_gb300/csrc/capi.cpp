@@ -90,6 +90,25 @@ struct Context {
   DevBuf src, t565, dst, scratch, rnd, err;
   DevBuf mips, blocks;  // s2tc_compress_dds: every level's pixels and blocks
   DevBuf rnd_win;       // the rand() stream position for the device generator
+  // pipelined tx_compress_dxtn: upload and download streams, per-range events
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, encode_stream = nullptr;
+  static constexpr int kPipeRanges = 64;
+  cudaEvent_t pipe_in[kPipeRanges] = {}, pipe_mid[kPipeRanges] = {}, pipe_out[kPipeRanges] = {};
+  bool pipe_ready = false;
+  bool init_pipe() {
+    if (pipe_ready) return true;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&encode_stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+      return false;
+    for (int i = 0; i < kPipeRanges; ++i)
+      if (!cuda_ok(cudaEventCreateWithFlags(&pipe_in[i], cudaEventDisableTiming), "cudaEventCreate") ||
+          !cuda_ok(cudaEventCreateWithFlags(&pipe_mid[i], cudaEventDisableTiming), "cudaEventCreate") ||
+          !cuda_ok(cudaEventCreateWithFlags(&pipe_out[i], cudaEventDisableTiming), "cudaEventCreate"))
+        return false;
+    pipe_ready = true;
+    return true;
+  }
   PinnedBuf host_rnd, host_out;
 
   bool init() {
@@ -320,6 +339,141 @@ int check_error_flag(Context& c, cudaStream_t s) {
   return ST_OK;
 }
 
+bool host_pinned(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// tx_compress_dxtn on a large image, pipelined: the image goes up in ranges of
+// whole dither tiles on one copy stream; the dither stream scans each range
+// as it lands (the scan's look-back reaches into the ranges before it); an
+// encode stream encodes the block rows whose four texel rows are complete
+// while the next range is dithered; a second copy stream brings those rows
+// back (per range when `dest` is pinned, else at the end).  Same kernels and
+// bytes as the unpipelined path.  Returns false when the image does not
+// qualify (the caller then takes that path).
+constexpr long long kPipeMinTexels = 1ll << 22;
+constexpr long long kPipeRangeTiles = 128;
+
+bool compress_host_pipelined(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
+                             unsigned char* dest, long long diff, const s2tc_options& opt, bool* done) {
+  *done = false;
+  const long long npx = (long long)width * height;
+  if (npx < kPipeMinTexels || opt.dither == DI_FLOYDSTEINBERG || diff < 0) return false;
+  const bool normal = normal_mode(opt);
+  const int per_block = rand_per_block(opt, dxt);
+  if (per_block > 0 && !rand_usable()) return false;
+  if (!c.init_pipe()) return false;
+  *done = true;
+  cudaStream_t s = c.stream, se = c.encode_stream;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
+  const long long row_bytes = (long long)bw * bs;
+  const long long tile = dither_tile_texels();
+  const long long tiles = (npx + tile - 1) / tile;
+  const long long per_range = std::max(kPipeRangeTiles, (tiles + Context::kPipeRanges - 1) / Context::kPipeRanges);
+  const int ranges = int((tiles + per_range - 1) / per_range);
+  if (!c.src.reserve(size_t(npx) * sc + 16, "cudaMalloc(src)")) return true;
+  if (!c.dst.reserve(size_t(row_bytes) * bh + 16, "cudaMalloc(dst)")) return true;
+  if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return true;
+  if (!c.scratch.reserve(dither_scratch_bytes(npx), "cudaMalloc(scratch)")) return true;
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return true;
+  if (!cuda_ok(cudaStreamWaitEvent(c.copy_in, c.arena_free, 0), "cudaStreamWaitEvent")) return true;
+  const bool pinned_out = host_pinned(dest);
+  uint8_t* d_src = c.src.as<uint8_t>();
+  uint8_t* d_dst = c.dst.as<uint8_t>();
+  // random-candidate words: the whole call's share of libc's stream, on the device
+  const uint32_t* rnd = nullptr;
+  if (per_block > 0) {
+    const long long words = (long long)bw * bh * per_block;
+    RandWindow win;
+    if (!c.rnd.reserve(size_t(words) * 4, "cudaMalloc(rand)") ||
+        !c.rnd_win.reserve(sizeof(RandWindow), "cudaMalloc(rand window)"))
+      return true;
+    if (!rand_take(words, &win)) {
+      set_error("libc rand() state could not be read");
+      return true;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(c.rnd_win.p, &win, sizeof(win), cudaMemcpyHostToDevice, s), "rand window upload") ||
+        !cuda_ok(rand_fill(c.rnd_win.as<RandWindow>(), c.rnd.as<uint32_t>(), words, s), "rand fill"))
+      return true;
+    rnd = c.rnd.as<uint32_t>();
+  }
+  DitherArgs da{};
+  da.src = d_src;
+  da.width = width;
+  da.height = height;
+  da.srccomps = sc;
+  da.alphabits = alpha_bits(dxt);
+  da.dst = c.t565.as<uint32_t>();
+  da.error = c.err.as<int>();
+  da.alpha_const = (1 << da.alphabits) - 1;
+  EncodeArgs ea{};
+  ea.t565 = c.t565.as<uint32_t>();
+  ea.width = width;
+  ea.height = height;
+  ea.bw = bw;
+  ea.bh = bh;
+  ea.dst = d_dst;
+  ea.pitch = row_bytes;
+  ea.aligned = 1;
+  ea.nrandom = opt.nrandom;
+  ea.prev_a1_first = -1;
+  if (dxt == DXT5 && normal && per_block == 0) {
+    ea.prev_a1_dev = c.err.as<int>() + 2;
+    ea.leftover_out = c.err.as<int>() + 2;
+  }
+  int rows_done = 0;
+  for (int r = 0; r < ranges; ++r) {
+    const long long t0 = r * per_range, t1 = std::min(tiles, t0 + per_range);
+    const long long p0 = t0 * tile, p1 = std::min(npx, t1 * tile);
+    if (!cuda_ok(cudaMemcpyAsync(d_src + p0 * sc, src + p0 * sc, size_t(p1 - p0) * sc, cudaMemcpyHostToDevice,
+                                 c.copy_in),
+                 "input upload") ||
+        !cuda_ok(cudaEventRecord(c.pipe_in[r], c.copy_in), "cudaEventRecord") ||
+        !cuda_ok(cudaStreamWaitEvent(s, c.pipe_in[r], 0), "cudaStreamWaitEvent") ||
+        !cuda_ok(launch_dither_range(da, opt.dither, c.scratch.as<uint8_t>(), t0, t1, s), "dither launch"))
+      return true;
+    const int rows_ready = r == ranges - 1 ? bh : int((p1 / width) / 4);
+    if (rows_ready <= rows_done) continue;
+    ea.by0 = rows_done;
+    ea.nby = rows_ready - rows_done;
+    ea.rnd = rnd ? rnd + (long long)rows_done * bw * per_block : nullptr;
+    if (!cuda_ok(cudaEventRecord(c.pipe_mid[r], s), "cudaEventRecord") ||
+        !cuda_ok(cudaStreamWaitEvent(se, c.pipe_mid[r], 0), "cudaStreamWaitEvent") ||
+        !cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, se), "encode launch"))
+      return true;
+    if (pinned_out) {
+      if (!cuda_ok(cudaEventRecord(c.pipe_out[r], se), "cudaEventRecord") ||
+          !cuda_ok(cudaStreamWaitEvent(c.copy_out, c.pipe_out[r], 0), "cudaStreamWaitEvent") ||
+          !cuda_ok(cudaMemcpy2DAsync(dest + (long long)rows_done * (row_bytes + diff), size_t(row_bytes + diff),
+                                     d_dst + (long long)rows_done * row_bytes, size_t(row_bytes), size_t(row_bytes),
+                                     size_t(rows_ready - rows_done), cudaMemcpyDeviceToHost, c.copy_out),
+                   "output download"))
+        return true;
+    }
+    rows_done = rows_ready;
+  }
+  // the compute stream joins the encode stream, then (unpinned output) downloads
+  if (!cuda_ok(cudaEventRecord(c.pipe_mid[0], se), "cudaEventRecord") ||
+      !cuda_ok(cudaStreamWaitEvent(s, c.pipe_mid[0], 0), "cudaStreamWaitEvent"))
+    return true;
+  if (!pinned_out &&
+      !cuda_ok(cudaMemcpy2DAsync(dest, size_t(row_bytes + diff), d_dst, size_t(row_bytes), size_t(row_bytes),
+                                 size_t(bh), cudaMemcpyDeviceToHost, s),
+               "output download"))
+    return true;
+  if (!cuda_ok(cudaEventRecord(c.pipe_out[0], c.copy_out), "cudaEventRecord") ||
+      !cuda_ok(cudaStreamWaitEvent(s, c.pipe_out[0], 0), "cudaStreamWaitEvent") ||
+      !cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord"))
+    return true;
+  check_error_flag(c, s);
+  return true;
+}
+
 // Host-memory compression used by tx_compress_dxtn.
 void compress_host(int srccomps, int width, int height, const unsigned char* src, int dxt, unsigned char* dest,
                    int dstRowStride, const s2tc_options& opt) {
@@ -327,6 +481,15 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
   std::lock_guard<std::mutex> lock(c.mu);
   if (!c.init()) return;
   cudaStream_t s = c.stream;
+  {
+    const int bs0 = block_bytes(dxt);
+    const long long diff0 = dstRowStride >= width * (bs0 / 4)
+                                ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs0 / 4)
+                                : 0;
+    bool done = false;
+    compress_host_pipelined(c, srccomps == 3 ? 3 : 4, width, height, src, dxt, dest, diff0, opt, &done);
+    if (done) return;
+  }
   const int sc = srccomps == 3 ? 3 : 4;
   const size_t in_bytes = size_t(width) * height * sc;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);

@@ -628,8 +628,8 @@ __global__ void __launch_bounds__(kThreads, S2TC_DITHER_MINBLOCKS) k_dither_simp
   if (t == 0) s_ticket = atomicAdd(w.ticket, 1u);
   bulk_init(sm);
   __syncthreads();
-  const long long g = s_ticket;
-  if (g >= w.total_tiles) return;
+  if ((long long)s_ticket >= w.total_tiles) return;
+  const long long g = w.tile_base + s_ticket;
   const int item = tile_item(w, g);
   DitherItem it = w.single;
   if (w.items) it = w.items[item];
@@ -661,8 +661,8 @@ __global__ void __launch_bounds__(kThreads, S2TC_DITHER_MINBLOCKS) k_dither_simp
 __global__ void __launch_bounds__(kThreads) k_dither_none(DitherWork w) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* px = reinterpret_cast<uint32_t*>(smem_raw);
-  const long long g = blockIdx.x;
-  if (g >= w.total_tiles) return;
+  if ((long long)blockIdx.x >= w.total_tiles) return;
+  const long long g = w.tile_base + blockIdx.x;
   const int item = tile_item(w, g);
   DitherItem it = w.single;
   if (w.items) it = w.items[item];
@@ -703,7 +703,12 @@ size_t dither_batch_scratch_bytes(long long tiles) {
 
 size_t dither_scratch_bytes(long long npx) { return dither_batch_scratch_bytes((npx + kTile - 1) / kTile); }
 
-cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cudaStream_t s) {
+namespace {
+
+// Launches tiles [w.tile_base, w.tile_base + w.total_tiles) of a work list
+// whose scan state (status words, aggregate records, ticket) is laid out in
+// `scratch` for `all_tiles` tiles.
+cudaError_t launch_tiles(DitherWork w, int dither, uint8_t* scratch, long long all_tiles, cudaStream_t s) {
   if (w.total_tiles <= 0) return cudaSuccess;
   // the attribute is set once per process (the first call on any device)
   static const cudaError_t attr = [] {
@@ -718,10 +723,11 @@ cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cuda
     return cudaGetLastError();
   }
   w.status = reinterpret_cast<unsigned long long*>(scratch);
-  w.aggs = scratch + w.total_tiles * sizeof(unsigned long long);
-  uintptr_t tk = reinterpret_cast<uintptr_t>(w.aggs + w.total_tiles * kRec);
+  w.aggs = scratch + all_tiles * sizeof(unsigned long long);
+  uintptr_t tk = reinterpret_cast<uintptr_t>(w.aggs + all_tiles * kRec);
   w.ticket = reinterpret_cast<unsigned int*>((tk + 15) & ~uintptr_t(15));
-  cudaError_t e = cudaMemsetAsync(w.status, 0, w.total_tiles * sizeof(unsigned long long), s);
+  cudaError_t e =
+      cudaMemsetAsync(w.status + w.tile_base, 0, w.total_tiles * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(w.ticket, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
@@ -730,18 +736,40 @@ cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cuda
   return cudaGetLastError();
 }
 
-cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream_t s) {
-  const long long npx = (long long)a.width * a.height;
-  if (npx <= 0) return cudaSuccess;
-  a.alpha_const = (1 << a.alphabits) - 1;
-  if (dither == DI_FLOYDSTEINBERG) return launch_dither_fs(a, scratch, s);
+DitherWork single_work(DitherArgs a) {
   DitherWork w{};
   w.items = nullptr;
   w.tile_offsets = nullptr;
   w.nitems = 1;
   w.single = DitherItem{a.src, a.width, a.height, a.srccomps == 3 ? 3 : 4, a.alphabits, a.dst};
-  w.total_tiles = (npx + kTile - 1) / kTile;
   w.error = a.error;
+  return w;
+}
+
+}  // namespace
+
+cudaError_t launch_dither_batch(DitherWork w, int dither, uint8_t* scratch, cudaStream_t s) {
+  w.tile_base = 0;
+  return launch_tiles(w, dither, scratch, w.total_tiles, s);
+}
+
+cudaError_t launch_dither_range(DitherArgs a, int dither, uint8_t* scratch, long long t0, long long t1,
+                                cudaStream_t s) {
+  const long long npx = (long long)a.width * a.height;
+  if (npx <= 0 || t1 <= t0) return cudaSuccess;
+  DitherWork w = single_work(a);
+  w.tile_base = t0;
+  w.total_tiles = t1 - t0;
+  return launch_tiles(w, dither, scratch, (npx + kTile - 1) / kTile, s);
+}
+
+cudaError_t launch_dither(DitherArgs a, int dither, uint8_t* scratch, cudaStream_t s) {
+  const long long npx = (long long)a.width * a.height;
+  if (npx <= 0) return cudaSuccess;
+  a.alpha_const = (1 << a.alphabits) - 1;
+  if (dither == DI_FLOYDSTEINBERG) return launch_dither_fs(a, scratch, s);
+  DitherWork w = single_work(a);
+  w.total_tiles = (npx + kTile - 1) / kTile;
   return launch_dither_batch(w, dither, scratch, s);
 }
 

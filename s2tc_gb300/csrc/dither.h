@@ -40,7 +40,8 @@ struct DitherWork {
   const long long* tile_offsets;  // device array, nitems entries
   int nitems;
   DitherItem single;
-  long long total_tiles;
+  long long total_tiles;         // tiles of this launch
+  long long tile_base;           // global index of its first tile (0 unless a launch covers a range)
   int* error;
   unsigned long long* status;   // total_tiles status words (zeroed before launch)
   uint8_t* aggs;                // total_tiles aggregate tables
@@ -55,6 +56,14 @@ long long dither_tile_texels();
 size_t dither_scratch_bytes(long long npx);
 size_t dither_batch_scratch_bytes(long long tiles);
 size_t dither_fs_scratch_bytes(int width, int height);
+
+// DITHER_NONE / DITHER_SIMPLE over tiles [t0, t1) of one image only, for
+// pipelined callers that launch an image's tiles in order, range by range, on
+// one stream (each range's look-back reaches into the earlier ranges).
+// `scratch` holds dither_scratch_bytes for the whole image; the first range
+// must start at tile 0.
+cudaError_t launch_dither_range(DitherArgs a, int dither, uint8_t* scratch, long long t0, long long t1,
+                                cudaStream_t s);
 
 // Runs the reference's rgb565_image for `dither` (DI_NONE, DI_SIMPLE or
 // DI_FLOYDSTEINBERG) on stream `s`.  `scratch` must hold the larger of the two

@@ -397,3 +397,33 @@ def test_launch_layouts_same_bytes(lib, oracle):
         assert x == pyoracle.libc_rand()
         a = gpu_compress(4, w, h, img, fmt, 1, metric, nr, refine, seed=3)
         assert np.array_equal(a, want), hex(fmt)
+
+
+def test_pipelined_host_path(lib):
+    """Large tx_compress_dxtn calls upload, dither, encode and download in
+    overlapping ranges: the bytes equal the device API's (one launch per
+    stage), for RGB and RGBA input, padded output rows, every dither it
+    covers and the device rand() stream."""
+    torch = pytest.importorskip("torch")
+    w, h = 2052, 2050  # 4.2 M texels, edge blocks on both sides
+    for sc, fmt, dither, metric, nr, refine, stride in ((4, 0x83F3, 1, 3, 0, 2, 0), (3, 0x83F1, 0, 5, -1, 1, 0),
+                                                         (4, 0x83F1, 1, 7, 8, 1, 0), (4, 0x83F2, 1, 5, -1, 1, 9000)):
+        img = workloads.value_noise_rgba(90 + sc, w, h)[:, :, :sc].copy().reshape(-1)
+        dest = np.zeros(((h + 3) // 4) * stride, np.uint8) if stride else None
+        a = gpu_compress(sc, w, h, img, fmt, dither, metric, nr, refine, seed=13, stride=stride, dest=dest)
+        after = pyoracle.libc_rand()
+        opt = s2.options(dither, metric, nr, refine)
+        d_src = torch.from_numpy(img).cuda()
+        bs = 8 if fmt == 0x83F1 else 16
+        row = ((w + 3) // 4) * bs
+        d_dst = torch.zeros(row * ((h + 3) // 4), dtype=torch.uint8, device="cuda")
+        pyoracle.srand(13)
+        s2.gpu_compress(sc, w, h, d_src, fmt, d_dst, opt=opt)
+        s2.gpu_synchronize(None)
+        assert after == pyoracle.libc_rand(), hex(fmt)
+        b = d_dst.cpu().numpy()
+        if stride:
+            got = a.reshape(-1)[: ((h + 3) // 4) * stride].reshape(-1, stride)[:, :row].reshape(-1)
+            assert np.array_equal(got, b), (sc, hex(fmt), stride)
+        else:
+            assert np.array_equal(a, b), (sc, hex(fmt), dither, metric, nr)
