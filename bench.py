@@ -475,6 +475,24 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     t_e2e = time.perf_counter() - t0
     libc_batch.close()
 
+    # the same images through the reference-compatible entry point, one
+    # synchronous tx_compress_dxtn call per image (host buffers)
+    s2.set_env(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+    lib = s2.load()
+    host_dst = [torch.empty(im["dst"].numel(), dtype=torch.uint8).pin_memory() for im in images]
+
+    def per_image_host():
+        for im, hs, hd in zip(images, host_src, host_dst):
+            lib.tx_compress_dxtn(im["srccomps"], im["width"], im["height"], hs.data_ptr(), im["format"],
+                                 hd.data_ptr(), 0)
+
+    per_image_host()
+    t0 = time.perf_counter()
+    host_passes = max(1, args.steps // 5)
+    for _ in range(host_passes):
+        per_image_host()
+    t_host = (time.perf_counter() - t0) / host_passes
+
     cpu = None
     if not args.no_cpu_baseline:
         # the CPU port on a bounded sample: the first levels until ~1.5 M
@@ -519,6 +537,9 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
             "per_image": {"value": single, "unit": "texels/s", "ms_per_step": 1000 * t_single / args.steps,
                           "launches_per_step": None},
             "batched_over_per_image": value / single, "bit_exact_batched_vs_per_image": bit_exact,
+            "per_image_tx_compress_dxtn": {"value": texels / t_host, "unit": "texels/s", "ms_per_step": 1000 * t_host,
+                                           "note": "one synchronous call per image, pinned host buffers"},
+            "e2e_over_per_image_tx_compress_dxtn": (args.steps * texels / t_e2e) / (texels / t_host),
             "e2e": {"value": args.steps * texels / t_e2e, "unit": "texels/s",
                     "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes,
                     "rand": "libc rand() stream, generated on the device",
