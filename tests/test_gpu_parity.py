@@ -123,6 +123,18 @@ def test_rgb565_image_many_tiles(lib, oracle, dither):
             assert np.array_equal(a, b), (w, h, sc, ab)
 
 
+def test_fs_strip_edges(lib, oracle):
+    """Floyd-Steinberg heights around the 32-row strips, odd widths (unaligned
+    rows), one-row and one-column images, all alpha variants."""
+    rng = np.random.default_rng(77)
+    for w, h in ((31, 32), (33, 64), (64, 33), (2, 129), (1, 100), (100, 1), (7, 31), (5, 63), (130, 96)):
+        for sc, ab in ((4, 1), (4, 4), (4, 8), (3, 1), (3, 4)):
+            img = cases.image(rng, w, h, sc, 0)
+            a = s2.rgb565_image(img, w, h, sc, ab, 2)
+            b = oracle.rgb565_image(img, w, h, sc, ab, 2)
+            assert np.array_equal(a, b), (w, h, sc, ab)
+
+
 def test_row_stride(lib, oracle):
     rng = np.random.default_rng(5)
     for fmt in cases.FORMATS:
