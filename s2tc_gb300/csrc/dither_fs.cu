@@ -2,29 +2,36 @@
 // 1350-1411) as a wavefront of warps.
 //
 // Texel (x, y) needs the error of (x-1, y) and of (x-1..x+1, y-1), so row y can
-// run two texels behind row y-1.  One warp owns a strip of 32 rows, one lane
-// per row: at step t lane r handles x = t - 2r.  Each lane keeps the errors it
-// sends to the row below in a two-entry window; the entry for x-1 is complete
-// once texel x has sent its 3/16 share, and one warp shuffle per channel and
-// step hands it to the lane below, which needs it one step later.
+// run two texels behind row y-1.  Rows are cut into strips of 32, and one warp
+// runs one channel of one strip, one lane per row: at step t lane r handles
+// x = t - 2r.  Each lane keeps the errors it sends to the row below in a
+// two-entry window; the entry for x-1 is complete once texel x has sent its
+// 3/16 share, and one warp shuffle per step hands it to the lane below, which
+// needs it one step later.  The three colour channels are independent chains,
+// so a strip's red, green and blue run as three warps of one CTA; they drop
+// their 5/6/5-bit values into a shared ring of texel words that the CTA writes
+// out every 32 steps.
 //
-// Strips are chained through carry rows in global memory.  The strip's last
-// lane writes every completed down-going entry as one tagged word (value plus a
-// bias, so that zero means "not written yet"); lane 0 of the next strip reads
-// the entries four at a time, two groups of four steps ahead, and spins
-// (bounded) only when a word is still zero.  No fences are needed: every word
-// is checked on its own.  Warps take tickets in launch order, so a strip only
-// waits on a strip that is already running.
+// Strips are chained through carry rows in global memory, one per channel.
+// The strip's last lane writes every completed down-going entry as one tagged
+// word (value plus a bias, so that zero means "not written yet"); lane 0 of
+// the next strip reads them a group of eight steps ahead (the source texels
+// three groups ahead), and spins (bounded) only when a word is still zero.
+// No fences are needed: every word is checked on its own.  CTAs (colour
+// pass) or warps (alpha pass) take tickets in launch order, so a strip only
+// waits on a strip that is already running.  No lane ever branches on its
+// own: loads are clamped into the image, stores are predicated, and every
+// wait is taken by the whole warp.
 //
-// The alpha channel of 1- and 4-bit alpha runs as a second launch of the same
-// kernel over one channel.  Like the reference, it starts from what the red
-// pass left in its first error row (s2tc_algorithm.cpp:1354, 1380-1382): the
-// red errors of the last row when its index is even, else the red errors it
-// sent below.  The red pass writes that row, tagged, as the alpha pass's first
-// carry row.
+// 1- and 4-bit alpha runs as a second launch, one warp per strip.  Like the
+// reference, it starts from what the red pass left in its first error row
+// (s2tc_algorithm.cpp:1354, 1380-1382): the red errors of the last row when
+// its index is even, else the red errors it sent below.  The red warp of the
+// last strip writes that row, tagged, as the alpha pass's first carry row.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "dither.h"
 
@@ -32,39 +39,49 @@ namespace s2tc {
 namespace {
 
 constexpr int kLanes = 32;           // rows per strip
-constexpr int kWarps = 4;            // strips per CTA
-constexpr int kGroup = 4;            // steps per group
-constexpr int kSpinLimit = 1 << 22;  // polls of one carry group
+constexpr int kGroup = 8;            // steps per group
+constexpr int kStages = 4;           // source texel stages: loads run kStages-1 groups ahead
+constexpr int kWindow = 32;          // steps between writes of the texel ring
+constexpr int kRing = 2 * kWindow;   // texels per row in the ring
+constexpr int kRingStride = kRing + 1;  // words per ring row (no bank conflicts)
+constexpr int kAlphaWarps = 4;       // strips per CTA of the alpha pass
+constexpr int kSpinLimit = 1 << 22;  // polls of one carry word
 constexpr int kTagBias = 0x40000000; // carry word = value + bias; 0 = not written
 
-// q * 4095 / 31 for q in [0, 31] as one multiply and shift.
-constexpr int kLoop31Mul = 8657095;
-constexpr bool loop31_exact() {
-  for (int q = 0; q <= 31; ++q)
-    if (((q * kLoop31Mul) >> 16) != q * 4095 / 31) return false;
+// q * 4095 / maxv for q in [0, maxv] as one multiply and shift by 16.
+__host__ __device__ constexpr int loop_mul(int maxv) { return maxv == 31 ? 8657095 : (4095 / maxv) << 16; }
+constexpr bool loop_exact(int maxv) {
+  for (int q = 0; q <= maxv; ++q)
+    if (((q * loop_mul(maxv)) >> 16) != q * 4095 / maxv) return false;
   return true;
 }
-static_assert(loop31_exact(), "loop31 multiplier");
-static_assert(4095 % 63 == 0 && 4095 % 15 == 0, "exact loops");
+static_assert(loop_exact(31) && loop_exact(63) && loop_exact(15), "loop multipliers");
+static_assert(kWindow % kGroup == 0, "window of whole groups");
+
+// A channel's quantiser: q = clamp(v >> (shift + 4), 0, maxv) on 12-bit values,
+// or the 1-bit variant (maxv 1).
+struct Quant {
+  int shift, maxv, mul;
+};
 
 struct FsOut {
   int q, e7, e3, e5, e1;
 };
 
 // One Floyd-Steinberg step on 12-bit values (s2tc_algorithm.cpp:1218-1261);
-// MAXV == 1 is the 1-bit variant (:1241).  `s12` is the source byte widened to
-// 12 bits, (s << 4) | (s >> 4).  The error shares are zero when `act` is false.
-template <int SHIFT, int MAXV>
-__device__ __forceinline__ FsOut fs_step(int err_in, int s12, bool act) {
+// BIT1 is the 1-bit variant (:1241).  `v` is the source byte widened to 12
+// bits, (s << 4) | (s >> 4), plus the error that reached the texel.  The error
+// shares are zero when `act` is false.
+template <bool BIT1>
+__device__ __forceinline__ FsOut fs_step(int v, bool act, const Quant& qt) {
   FsOut o;
-  const int v = s12 + err_in;
   int loop;
-  if (MAXV == 1) {
+  if (BIT1) {
     o.q = v >= 2048;
     loop = o.q ? 4095 : 0;
   } else {
-    o.q = min(max(v >> (SHIFT + 4), 0), MAXV);
-    loop = MAXV == 31 ? (o.q * kLoop31Mul) >> 16 : o.q * (4095 / MAXV);
+    o.q = min(max(v >> (qt.shift + 4), 0), qt.maxv);
+    loop = (o.q * qt.mul) >> 16;
   }
   int e = act ? v - loop : 0;
   o.e7 = (e * 7 + 8) / 16;
@@ -96,80 +113,121 @@ struct FsArgs {
   uint32_t* dst;
   int width, height;
   int nstrips;
-  int wpad;             // carry row length, width rounded up to 4
-  int* carry;           // nstrips * NCH rows; strip s reads rows s*NCH.. (strip 0's only if seeded)
-  int* leftover;        // red pass followed by an alpha pass: the alpha pass's first carry row
+  int wpad;             // carry row length, width rounded up to a whole group
+  int* carry;           // nstrips * channels rows; strip s, channel c reads row s * channels + c
+  int* leftover;        // colour pass followed by an alpha pass: the alpha pass's first carry row
   int seeded;           // alpha pass: strip 0 reads its carry row (the red leftover)
   int src8, dst8;       // 8-byte aligned base pointers
   unsigned int* ticket;
   int* error;
 };
 
-// NCH == 3: red/green/blue pass.  For 3-component input AP is the constant
-// alpha byte; for 4 components AP == 255 copies the source alpha (8-bit alpha)
-// and AP == 0 leaves 0 for the alpha pass.  NCH == 1: alpha pass with AP alpha
-// bits (1 or 4), writing byte 3 only.
-template <int NCH, int SC, int AP>
-struct Strip {
-  FsArgs a;
-  int lane, y, w;
-  bool row_ok, al_src, al_dst, has_in;
-  const int* cin;          // carry rows read by lane 0
-  int* emit;               // carry rows written by the emitting lane, or null
-  int emit_lane, emit_nch, emit_err;  // emit_err: write err_in (not the window) at x
+// One channel of one strip, one lane per row, reading source byte `srcb`
+// (3 for alpha) of SC-byte texels.
+template <bool BIT1, int SC>
+struct Chan {
+  Quant qt;
+  int srcb;
+  int lane, w;
+  bool row_ok, has_in;
+  int wpad_end;            // last aligned group start inside the carry row
   const uint8_t* srow;
-  uint32_t* drow;
+  const int* cin;          // carry row read by lane 0
+  int* emit;               // carry row written by lane emit_lane, or null
+  int emit_lane;
+  bool emit_err;           // write the texel's own error at x (red leftover of an even last row)
+  int* error;
 
-  uint32_t inb[3][kGroup];     // source texels of three groups
-  int cinb[3][NCH][kGroup];    // lane 0: carry entries of three groups
-  int pa[NCH];                 // error of the texel at hand (minus the carry, lane 0)
-  int wa[NCH], wb[NCH];        // down-going errors for x-1 and x
+  uint32_t inb[kStages][kGroup];  // source texels of kStages groups (SC 4: whole words)
+  int cinb[2][kGroup];            // carry entries of this group and the next (lane 0; 0 elsewhere)
+  int pa, wa, wb;           // error of the texel at hand (carry aside); down-going x-1, x
+  int q[kGroup];            // quantised values of the group
+  bool pairs;               // 8-byte source loads (SC 4, every row start 8-byte aligned)
+  bool words;               // 4-byte source loads (SC 4, 4-byte aligned source)
 
+  __device__ __forceinline__ void setup(const FsArgs& a, int strip, int ch, int nch, bool red_leftover, Quant q,
+                                        int sb) {
+    qt = q;
+    srcb = sb;
+    w = a.width;
+    error = a.error;
+    wpad_end = a.wpad - kGroup;
+    lane = threadIdx.x & 31;
+    const int y = strip * kLanes + lane;
+    row_ok = y < a.height;
+    srow = a.src + size_t(row_ok ? y : 0) * w * SC;
+    words = SC == 4 && (reinterpret_cast<uintptr_t>(a.src) & 3) == 0;
+    pairs = words && a.src8 && (w & 1) == 0;
+    has_in = strip > 0 || a.seeded;
+    cin = a.carry + (size_t(strip) * nch + ch) * a.wpad;
+    emit = nullptr;
+    emit_lane = -1;
+    emit_err = false;
+    if (strip + 1 < a.nstrips) {
+      emit = a.carry + (size_t(strip + 1) * nch + ch) * a.wpad;
+      emit_lane = kLanes - 1;
+    } else if (red_leftover) {
+      emit = a.leftover;
+      emit_lane = a.height - 1 - strip * kLanes;
+      emit_err = ((a.height - 1) & 1) == 0;
+    }
+    pa = wa = wb = 0;
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) cinb[0][k] = cinb[1][k] = 0;
+#pragma unroll
+    for (int st = 0; st + 1 < kStages; ++st) load_src(st, st);
+    load_cin(0, 0);
+  }
+
+  // Source texels of group g into stage st.  The loads are unconditional (x
+  // clamped into the row; rows past the image read row 0) so that no lane
+  // branches around them: a texel outside the image only feeds a step that
+  // does nothing.
   __device__ __forceinline__ void load_src(int st, int g) {
     const int x0 = g * kGroup - 2 * lane;
-    if (SC == 4) {
-      if (row_ok && x0 >= 0 && x0 + kGroup <= w && al_src) {
-        const uint2 p0 = __ldg(reinterpret_cast<const uint2*>(srow + size_t(x0) * 4));
-        const uint2 p1 = __ldg(reinterpret_cast<const uint2*>(srow + size_t(x0) * 4 + 8));
-        inb[st][0] = p0.x;
-        inb[st][1] = p0.y;
-        inb[st][2] = p1.x;
-        inb[st][3] = p1.y;
-      } else {
+    if (pairs) {
 #pragma unroll
-        for (int k = 0; k < kGroup; ++k) {
-          const int x = x0 + k;
-          inb[st][k] = row_ok && unsigned(x) < unsigned(w) ? __ldg(reinterpret_cast<const uint32_t*>(srow + size_t(x) * 4)) : 0u;
-        }
+      for (int h = 0; h < kGroup / 2; ++h) {
+        const int x = min(max(x0 + 2 * h, 0), w - 2);
+        const uint2 p = __ldg(reinterpret_cast<const uint2*>(srow + size_t(x) * 4));
+        inb[st][2 * h] = p.x;
+        inb[st][2 * h + 1] = p.y;
+      }
+    } else if (words) {
+#pragma unroll
+      for (int k = 0; k < kGroup; ++k) {
+        const int x = min(max(x0 + k, 0), w - 1);
+        inb[st][k] = __ldg(reinterpret_cast<const uint32_t*>(srow + size_t(x) * 4));
+      }
+    } else if (SC == 4) {
+#pragma unroll
+      for (int k = 0; k < kGroup; ++k) {
+        const uint8_t* p = srow + size_t(min(max(x0 + k, 0), w - 1)) * 4;
+        inb[st][k] = uint32_t(__ldg(p)) | (uint32_t(__ldg(p + 1)) << 8) | (uint32_t(__ldg(p + 2)) << 16) |
+                     (uint32_t(__ldg(p + 3)) << 24);
       }
     } else {
 #pragma unroll
-      for (int k = 0; k < kGroup; ++k) {
-        const int x = x0 + k;
-        uint32_t v = 0;
-        if (row_ok && unsigned(x) < unsigned(w)) {
-          const uint8_t* s = srow + size_t(x) * 3;
-          v = uint32_t(__ldg(s)) | (uint32_t(__ldg(s + 1)) << 8) | (uint32_t(__ldg(s + 2)) << 16);
-        }
-        inb[st][k] = v;
-      }
+      for (int k = 0; k < kGroup; ++k) inb[st][k] = __ldg(srow + size_t(min(max(x0 + k, 0), w - 1)) * 3 + srcb);
     }
   }
 
+  __device__ __forceinline__ int src_byte(uint32_t v) const { return SC == 4 ? int((v >> (8 * srcb)) & 0xFF) : int(v); }
+
   // Carry words of group g into stage st.  All lanes load the same words (one
   // broadcast transaction) so that the warp never splits; only lane 0 keeps
-  // them once their tags are checked.
+  // them once their tags are checked.  Past the row's end the words are
+  // clamped into the carry row and never used.
   __device__ __forceinline__ void load_cin(int st, int g) {
     if (!has_in) return;
-    const int x0 = g * kGroup;
+    const int x0 = min(g * kGroup, wpad_end);
 #pragma unroll
-    for (int c = 0; c < NCH; ++c) {
-      int4 v = make_int4(0, 0, 0, 0);
-      if (x0 < w) v = __ldcg(reinterpret_cast<const int4*>(cin + size_t(c) * a.wpad + x0));
-      cinb[st][c][0] = v.x;
-      cinb[st][c][1] = v.y;
-      cinb[st][c][2] = v.z;
-      cinb[st][c][3] = v.w;
+    for (int h = 0; h < kGroup / 4; ++h) {
+      const int4 v = __ldcg(reinterpret_cast<const int4*>(cin + x0 + 4 * h));
+      cinb[st][4 * h] = v.x;
+      cinb[st][4 * h + 1] = v.y;
+      cinb[st][4 * h + 2] = v.z;
+      cinb[st][4 * h + 3] = v.w;
     }
   }
 
@@ -177,164 +235,176 @@ struct Strip {
     const int need = min(kGroup, w - g * kGroup);
     bool ok = true;
 #pragma unroll
-    for (int c = 0; c < NCH; ++c)
-#pragma unroll
-      for (int k = 0; k < kGroup; ++k) ok &= cinb[st][c][k] != 0 || k >= need;
+    for (int k = 0; k < kGroup; ++k) ok &= cinb[st][k] != 0 || k >= need;
     return ok;
   }
 
-  // Makes sure group g's carry words (stage ST) are written, then strips their
-  // tags (and zeroes them for every lane but 0).  A group that is not there
-  // yet means the prefetches of the next two groups are stale as well, so the
-  // wait runs until the producer is three groups further on and then reloads
-  // all three stages: that lag keeps later prefetches (issued two groups
-  // ahead) from coming back empty.  The branch is warp-uniform.
-  template <int ST>
+  // Makes sure group g's carry words (stage CS) are written, then strips their
+  // tags (and zeroes them for every lane but 0, and past the row's end).  A group that is not there
+  // yet means the prefetch of the next group is stale as well, so the wait
+  // runs until the producer is two groups further on and then reloads both
+  // stages: that lag keeps later prefetches (issued a group ahead) from
+  // coming back empty.  The branch is warp-uniform.
+  template <int CS>
   __device__ __forceinline__ void take_cin(int g) {
     if (!has_in) return;
     const int x0 = g * kGroup;
-    if (x0 >= w) return;
-    if (!cin_ready(ST, g)) {
-      const int xw = min(x0 + 4 * kGroup - 1, w - 1);  // last entry of group g+3
-      const int* pw = cin + size_t(NCH - 1) * a.wpad + xw;
+    if (x0 < w && !cin_ready(CS, g)) {
+      const int* pw = cin + min(x0 + 3 * kGroup - 1, w - 1);  // last entry of group g+2
       int spins = 0;
       while (ld_poll(pw) == 0 && ++spins < kSpinLimit)
-        if ((spins & 255) == 0 && ld_poll(a.error)) break;
+        if ((spins & 255) == 0 && ld_poll(error)) break;
       spins = 0;
       do {
-        load_cin(ST, g);
-        load_cin((ST + 1) % 3, g + 1);
-        load_cin((ST + 2) % 3, g + 2);
-      } while (!cin_ready(ST, g) && ++spins < 64 && !ld_poll(a.error));
-      if (!cin_ready(ST, g) && lane == 0) atomicExch(a.error, 1);
+        load_cin(CS, g);
+        load_cin(CS ^ 1, g + 1);
+      } while (!cin_ready(CS, g) && ++spins < 64 && !ld_poll(error));
+      if (!cin_ready(CS, g) && lane == 0) atomicExch(error, 1);
     }
 #pragma unroll
-    for (int c = 0; c < NCH; ++c)
-#pragma unroll
-      for (int k = 0; k < kGroup; ++k) cinb[ST][c][k] = lane == 0 && cinb[ST][c][k] ? cinb[ST][c][k] - kTagBias : 0;
+    for (int k = 0; k < kGroup; ++k)
+      cinb[CS][k] = lane == 0 && x0 + k < w && cinb[CS][k] ? cinb[CS][k] - kTagBias : 0;
   }
 
+  // The steps of group g (its source texels in stage ST); the quantised
+  // values land in q[].
   template <int ST>
-  __device__ __forceinline__ void group(int g) {
-    load_src((ST + 2) % 3, g + 2);
-    load_cin((ST + 2) % 3, g + 2);
-    take_cin<ST>(g);
+  __device__ __forceinline__ void steps(int g) {
+    constexpr int CS = ST & 1;
+    load_src((ST + kStages - 1) % kStages, g + kStages - 1);
+    load_cin(CS ^ 1, g + 1);
+    take_cin<CS>(g);
     const int x0 = g * kGroup - 2 * lane;
-    uint32_t out[kGroup];
+    int ev[kGroup];
 #pragma unroll
     for (int k = 0; k < kGroup; ++k) {
       const int x = x0 + k;
       const bool act = row_ok && unsigned(x) < unsigned(w);
-      const uint32_t texel = inb[ST][k];
-      // the emitting lane writes the entry for x-1 (complete now) or, for the
-      // red leftover of an even last row, this texel's error
-      const bool em = lane == emit_lane && (emit_err ? act : unsigned(x - 1) < unsigned(w));
-      int* const ep = emit + (emit_err ? x : x - 1);
-      uint32_t word = 0;
-#pragma unroll
-      for (int c = 0; c < NCH; ++c) {
-        const int ein = pa[c] + cinb[ST][c][k];
-        FsOut f;
-        if (NCH == 1) {
-          const int s12 = widen12(texel >> 24);
-          f = AP == 1 ? fs_step<7, 1>(ein, s12, act) : fs_step<4, 15>(ein, s12, act);
-        } else {
-          const int s12 = widen12((texel >> (8 * c)) & 0xFF);
-          f = c == 1 ? fs_step<2, 63>(ein, s12, act) : fs_step<3, 31>(ein, s12, act);
-        }
-        word |= uint32_t(f.q) << (8 * c);
-        // the entry for x-1 is complete; x and x+1 move up the window
-        const int down = wa[c] + f.e3;
-        wa[c] = wb[c] + f.e5;
-        wb[c] = f.e1;
-        const int up = __shfl_up_sync(0xffffffffu, down, 1);
-        pa[c] = f.e7 + (lane ? up : 0);
-        st_tagged_if(em && c < emit_nch, ep + size_t(c) * a.wpad, emit_err ? ein : down);
-      }
-      if (NCH == 3) {
-        if (SC == 3) word |= uint32_t(AP) << 24;
-        else if (AP == 255) word |= texel & 0xFF000000u;
-      }
-      out[k] = word;
+      const int ein = pa + cinb[CS][k];
+      const FsOut f = fs_step<BIT1>(widen12(src_byte(inb[ST][k])) + ein, act, qt);
+      q[k] = f.q;
+      // the entry for x-1 is complete; x and x+1 move up the window
+      const int down = wa + f.e3;
+      wa = wb + f.e5;
+      wb = f.e1;
+      const int up = __shfl_up_sync(0xffffffffu, down, 1);
+      pa = f.e7 + (lane ? up : 0);
+      ev[k] = emit_err ? ein : down;
     }
-    // store the group's texels
-    if (NCH == 3) {
-      if (row_ok && x0 >= 0 && x0 + kGroup <= w && al_dst) {
-        uint2* d = reinterpret_cast<uint2*>(drow + x0);
-        d[0] = make_uint2(out[0], out[1]);
-        d[1] = make_uint2(out[2], out[3]);
-      } else {
+    // the emitting lane writes the group's completed entries: x-1 for each
+    // texel x, or (red leftover, even last row) each texel's own error
+    if (emit) {
+      const int i0 = emit_err ? x0 : x0 - 1;
+      const bool me = lane == emit_lane;
 #pragma unroll
-        for (int k = 0; k < kGroup; ++k)
-          if (row_ok && unsigned(x0 + k) < unsigned(w)) drow[x0 + k] = out[k];
-      }
-    } else {
-      uint8_t* d = reinterpret_cast<uint8_t*>(drow);
-#pragma unroll
-      for (int k = 0; k < kGroup; ++k)
-        if (row_ok && unsigned(x0 + k) < unsigned(w)) d[size_t(x0 + k) * 4 + 3] = uint8_t(out[k]);
-    }
-  }
-
-  __device__ __forceinline__ void run(int strip) {
-    w = a.width;
-    lane = threadIdx.x & 31;
-    y = strip * kLanes + lane;
-    row_ok = y < a.height;
-    const int yy = row_ok ? y : 0;
-    srow = a.src + size_t(yy) * w * SC;
-    drow = a.dst + size_t(yy) * w;
-    const bool odd_row_start = (yy & w & 1) != 0;  // y * w odd
-    al_src = a.src8 && !odd_row_start;
-    al_dst = a.dst8 && !odd_row_start;
-    has_in = strip > 0 || a.seeded;
-    cin = a.carry + size_t(strip) * NCH * a.wpad;
-    const bool last = strip == a.nstrips - 1;
-    emit = nullptr;
-    emit_lane = -1;
-    emit_nch = NCH;
-    emit_err = 0;
-    if (!last) {
-      emit = a.carry + size_t(strip + 1) * NCH * a.wpad;
-      emit_lane = kLanes - 1;
-    } else if (NCH == 3 && a.leftover) {
-      emit = a.leftover;
-      emit_lane = a.height - 1 - strip * kLanes;
-      emit_nch = 1;
-      emit_err = ((a.height - 1) & 1) == 0;
-    }
-#pragma unroll
-    for (int c = 0; c < NCH; ++c) pa[c] = wa[c] = wb[c] = 0;
-#pragma unroll
-    for (int st = 0; st < 3; ++st)
-#pragma unroll
-      for (int c = 0; c < NCH; ++c)
-#pragma unroll
-        for (int k = 0; k < kGroup; ++k) cinb[st][c][k] = 0;
-    load_src(0, 0);
-    load_src(1, 1);
-    load_cin(0, 0);
-    load_cin(1, 1);
-    // the last lane reaches x = w (where it completes the entry for w-1) at
-    // step w + 2 * 31
-    const int ngroups = (w + 2 * (kLanes - 1) + 1 + kGroup - 1) / kGroup;
-    for (int g = 0; g < ngroups; g += 3) {
-      group<0>(g);
-      if (g + 1 < ngroups) group<1>(g + 1);
-      if (g + 2 < ngroups) group<2>(g + 2);
+      for (int k = 0; k < kGroup; ++k) st_tagged_if(me && unsigned(i0 + k) < unsigned(w), emit + i0 + k, ev[k]);
     }
   }
 };
 
-template <int NCH, int SC, int AP>
-__global__ void __launch_bounds__(kLanes * kWarps) k_fs(FsArgs a) {
+// Colour pass: one CTA per strip, warp c runs channel c.  AP is the alpha
+// byte: for 3-component input the constant (1, 15 or 255); for 4 components
+// 255 copies the source alpha (8-bit alpha) and 0 leaves 0 for the alpha pass.
+template <int SC, int AP>
+__device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t (*ring)[kRingStride], int ch) {
+  const Quant qt = ch == 1 ? Quant{2, 63, loop_mul(63)} : Quant{3, 31, loop_mul(31)};
+  Chan<false, SC> c;
+  c.setup(a, strip, ch, 3, ch == 0 && a.leftover != nullptr, qt, ch);
+  const int lane = c.lane;
+  const int w = a.width;
+  const int y = strip * kLanes + lane;
+  const bool row_ok = y < a.height;
+  uint32_t* drow = a.dst + size_t(row_ok ? y : 0) * w;
+  const bool al_dst = a.dst8 && (((row_ok ? y : 0) & w & 1) == 0);
+  uint8_t* ring8 = reinterpret_cast<uint8_t*>(ring[lane]);
+  // the last lane reaches x = w (where it completes the entry for w-1) at
+  // step w + 2 * 31; whole windows so that every texel is written out
+  const int nsteps = w + 2 * (kLanes - 1) + 1;
+  const int ngroups = (nsteps + kWindow - 1) / kWindow * (kWindow / kGroup);
+
+  auto group = [&](auto stc, int g) {
+    constexpr int ST = decltype(stc)::value;
+    c.template steps<ST>(g);
+    const int x0 = g * kGroup - 2 * lane;
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k) {
+      const int pos = (x0 + k) & (kRing - 1);
+      ring8[pos * 4 + ch] = uint8_t(c.q[k]);
+      if (SC == 4 && AP == 255 && ch == 0) ring8[pos * 4 + 3] = uint8_t(c.inb[ST][k] >> 24);
+    }
+    if ((g + 1) % (kWindow / kGroup) == 0) {
+      // window m holds each lane's texels [32m - 2r, 32m + 32 - 2r); the ring
+      // keeps two windows, so one barrier per window is enough
+      asm volatile("bar.sync 1, 96;" ::: "memory");
+      const int xs = (g + 1) * kGroup - kWindow - 2 * lane;
+      for (int j = ch; j < kWindow / 2; j += 3) {
+        const int x = xs + 2 * j;
+        if (!row_ok || x < 0 || x >= w) continue;
+        uint32_t v0 = ring[lane][x & (kRing - 1)];
+        uint32_t v1 = ring[lane][(x + 1) & (kRing - 1)];
+        if (!(SC == 4 && AP == 255)) {
+          v0 = (v0 & 0x00FFFFFFu) | (uint32_t(AP) << 24);
+          v1 = (v1 & 0x00FFFFFFu) | (uint32_t(AP) << 24);
+        }
+        if (x + 1 < w && al_dst) {
+          *reinterpret_cast<uint2*>(drow + x) = make_uint2(v0, v1);
+        } else {
+          drow[x] = v0;
+          if (x + 1 < w) drow[x + 1] = v1;
+        }
+      }
+    }
+  };
+  for (int g = 0; g < ngroups; g += kStages) {
+    static_assert(kStages == 4, "stage unroll");
+    group(std::integral_constant<int, 0>(), g);
+    if (g + 1 < ngroups) group(std::integral_constant<int, 1>(), g + 1);
+    if (g + 2 < ngroups) group(std::integral_constant<int, 2>(), g + 2);
+    if (g + 3 < ngroups) group(std::integral_constant<int, 3>(), g + 3);
+  }
+}
+
+template <int SC, int AP>
+__global__ void __launch_bounds__(3 * kLanes, 1) k_fs_colour(FsArgs a) {
+  __shared__ uint32_t ring[kLanes][kRingStride];
+  __shared__ int s_strip;
+  if (threadIdx.x == 0) s_strip = int(atomicAdd(a.ticket, 1u));
+  __syncthreads();
+  const int strip = s_strip;
+  if (strip >= a.nstrips) return;
+  colour_warp<SC, AP>(a, strip, ring, threadIdx.x >> 5);
+}
+
+// Alpha pass: one warp per strip, writing byte 3 of each texel.
+template <int AB>
+__global__ void __launch_bounds__(kAlphaWarps * kLanes, 1) k_fs_alpha(FsArgs a) {
   int strip = 0;
   if ((threadIdx.x & 31) == 0) strip = int(atomicAdd(a.ticket, 1u));
   strip = __shfl_sync(0xffffffffu, strip, 0);
   if (strip >= a.nstrips) return;
-  Strip<NCH, SC, AP> s;
-  s.a = a;
-  s.run(strip);
+  Chan<AB == 1, 4> c;
+  c.setup(a, strip, 0, 1, false, Quant{4, 15, loop_mul(15)}, 3);
+  const int lane = c.lane;
+  const int w = a.width;
+  const int y = strip * kLanes + lane;
+  const bool row_ok = y < a.height;
+  uint8_t* d = reinterpret_cast<uint8_t*>(a.dst + size_t(row_ok ? y : 0) * w) + 3;
+  const int ngroups = (w + 2 * (kLanes - 1) + 1 + kGroup - 1) / kGroup;
+  auto group = [&](auto stc, int g) {
+    constexpr int ST = decltype(stc)::value;
+    c.template steps<ST>(g);
+    const int x0 = g * kGroup - 2 * lane;
+#pragma unroll
+    for (int k = 0; k < kGroup; ++k)
+      if (row_ok && unsigned(x0 + k) < unsigned(w)) d[size_t(x0 + k) * 4] = uint8_t(c.q[k]);
+  };
+  for (int g = 0; g < ngroups; g += kStages) {
+    static_assert(kStages == 4, "stage unroll");
+    group(std::integral_constant<int, 0>(), g);
+    if (g + 1 < ngroups) group(std::integral_constant<int, 1>(), g + 1);
+    if (g + 2 < ngroups) group(std::integral_constant<int, 2>(), g + 2);
+    if (g + 3 < ngroups) group(std::integral_constant<int, 3>(), g + 3);
+  }
 }
 
 struct FsLayout {
@@ -345,7 +415,7 @@ struct FsLayout {
 FsLayout fs_layout(int width, int height) {
   FsLayout l;
   l.nstrips = (height + kLanes - 1) / kLanes;
-  l.wpad = (width + 3) & ~3;
+  l.wpad = ((width + kGroup - 1) / kGroup) * kGroup;
   l.rgb_bytes = size_t(l.nstrips) * 3 * l.wpad * sizeof(int);
   l.alpha_bytes = size_t(l.nstrips) * l.wpad * sizeof(int);
   return l;
@@ -379,24 +449,23 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   a.dst8 = (reinterpret_cast<uintptr_t>(d.dst) & 7) == 0;
   a.ticket = tickets;
   a.error = d.error;
-  // the carry words of strip 0 are never read in the red/green/blue pass
+  // the carry rows of strip 0 are never read in the colour pass
   const size_t skip = size_t(l.wpad) * 3 * sizeof(int);
   cudaError_t e = cudaMemsetAsync(scratch + skip, 0, l.rgb_bytes - skip, s);
   if (e == cudaSuccess && alpha_pass) e = cudaMemsetAsync(alpha_carry, 0, l.alpha_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(tickets, 0, 2 * sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
-  const unsigned warps = unsigned(l.nstrips);
-  const unsigned grid = (warps + kWarps - 1) / kWarps;
-  const unsigned block = kLanes * kWarps;
+  const unsigned grid = unsigned(l.nstrips);
+  const unsigned block = 3 * kLanes;
   count_launches(1);
   if (d.srccomps == 3) {
-    if (d.alphabits == 1) k_fs<3, 3, 1><<<grid, block, 0, s>>>(a);
-    else if (d.alphabits == 4) k_fs<3, 3, 15><<<grid, block, 0, s>>>(a);
-    else k_fs<3, 3, 255><<<grid, block, 0, s>>>(a);
+    if (d.alphabits == 1) k_fs_colour<3, 1><<<grid, block, 0, s>>>(a);
+    else if (d.alphabits == 4) k_fs_colour<3, 15><<<grid, block, 0, s>>>(a);
+    else k_fs_colour<3, 255><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
   }
-  if (alpha_pass) k_fs<3, 4, 0><<<grid, block, 0, s>>>(a);
-  else k_fs<3, 4, 255><<<grid, block, 0, s>>>(a);
+  if (alpha_pass) k_fs_colour<4, 0><<<grid, block, 0, s>>>(a);
+  else k_fs_colour<4, 255><<<grid, block, 0, s>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess || !alpha_pass) return e;
   // alpha pass, seeded with the red leftover row
@@ -405,9 +474,10 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   b.leftover = nullptr;
   b.seeded = 1;
   b.ticket = tickets + 1;
+  const unsigned agrid = (unsigned(l.nstrips) + kAlphaWarps - 1) / kAlphaWarps;
   count_launches(1);
-  if (d.alphabits == 1) k_fs<1, 4, 1><<<grid, block, 0, s>>>(b);
-  else k_fs<1, 4, 4><<<grid, block, 0, s>>>(b);
+  if (d.alphabits == 1) k_fs_alpha<1><<<agrid, kAlphaWarps * kLanes, 0, s>>>(b);
+  else k_fs_alpha<4><<<agrid, kAlphaWarps * kLanes, 0, s>>>(b);
   return cudaGetLastError();
 }
 
