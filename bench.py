@@ -49,6 +49,10 @@ NIMG = 4
 WORKLOADS = {
     "value_noise_4096_dxt5_srgb_mixed_all16_loop": dict(
         w=4096, h=4096, sc=4, fmt=0x83F3, dither=1, metric=3, nrandom=0, refine=2, gen="value_noise", seed=2),
+    # the same texture with Floyd-Steinberg dither: a two-dimensional
+    # wavefront, latency-bound rather than bandwidth-bound
+    "value_noise_4096_dxt5_srgb_mixed_all16_loop_fs": dict(
+        w=4096, h=4096, sc=4, fmt=0x83F3, dither=2, metric=3, nrandom=0, refine=2, gen="value_noise", seed=2),
     "plain_1024_dxt1_wavg_quick_always": dict(
         w=1024, h=1024, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
     "plain_8192_dxt1_wavg_quick_always": dict(
@@ -1043,8 +1047,11 @@ def main() -> None:
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "peak_source": peak_note, "traffic": None,
                 "stage_ms_per_launch": {"dither": dit_launch_ms, "encode": enc_launch_ms},
-                "note": "the all-pairs search is integer-ALU bound; frac is of the HBM roofline for the "
-                        "algorithmic bytes"}
+                "note": ("the Floyd-Steinberg wavefront is latency-bound (a chain of width + 2 * height "
+                         "dependent steps); frac is of the HBM roofline for the algorithmic bytes")
+                if dominant == "dither" and wl["dither"] == 2 else
+                "the all-pairs search is integer-ALU bound; frac is of the HBM roofline for the "
+                "algorithmic bytes"}
     prof = ROOT / "profiles" / "traffic.json"
     if prof.exists():
         try:

@@ -15,8 +15,8 @@
 // Strips are chained through carry rows in global memory, one per channel.
 // The strip's last lane writes every completed down-going entry as one tagged
 // word (value plus a bias, so that zero means "not written yet"); lane 0 of
-// the next strip reads them a group of eight steps ahead (the source texels
-// three groups ahead), and spins (bounded) only when a word is still zero.
+// the next strip reads them (and its source texels) two groups of eight steps
+// ahead, and spins (bounded) only when a word is still zero.
 // No fences are needed: every word is checked on its own.  CTAs (colour
 // pass) or warps (alpha pass) take tickets in launch order, so a strip only
 // waits on a strip that is already running.  No lane ever branches on its
@@ -39,11 +39,15 @@ namespace s2tc {
 namespace {
 
 constexpr int kLanes = 32;           // rows per strip
+constexpr int kLag = 2;              // steps each row runs behind the row above
 constexpr int kGroup = 8;            // steps per group
-constexpr int kStages = 4;           // source texel stages: loads run kStages-1 groups ahead
+constexpr int kStages = 3;           // register stages: loads run kStages-1 groups ahead
 constexpr int kWindow = 32;          // steps between writes of the texel ring
 constexpr int kRing = 2 * kWindow;   // texels per row in the ring
-constexpr int kRingStride = kRing + 1;  // words per ring row (no bank conflicts)
+// words per ring row: lane r touches word r * stride + ((t - kLag * r) & 63) at
+// step t, so stride - kLag must be odd for the 32 lanes to hit 32 banks
+constexpr int kRingStride = kRing + 1;
+static_assert((kRingStride - kLag) % 2 == 1 && kLag % 2 == 0, "ring banks, texel pairs");
 constexpr int kAlphaWarps = 4;       // strips per CTA of the alpha pass
 constexpr int kSpinLimit = 1 << 22;  // polls of one carry word
 constexpr int kTagBias = 0x40000000; // carry word = value + bias; 0 = not written
@@ -63,6 +67,9 @@ static_assert(kWindow % kGroup == 0, "window of whole groups");
 struct Quant {
   int shift, maxv, mul;
 };
+
+__device__ __forceinline__ int widen12(uint32_t b) { return int((b << 4) | (b >> 4)); }
+
 
 struct FsOut {
   int q, e7, e3, e5, e1;
@@ -92,8 +99,6 @@ __device__ __forceinline__ FsOut fs_step(int v, bool act, const Quant& qt) {
   o.e1 = e - o.e5;
   return o;
 }
-
-__device__ __forceinline__ int widen12(uint32_t b) { return int((b << 4) | (b >> 4)); }
 
 // Stores v (tagged) at p when `on`; one predicated store, no branch.
 __device__ __forceinline__ void st_tagged_if(bool on, int* p, int v) {
@@ -139,8 +144,10 @@ struct Chan {
   int* error;
 
   uint32_t inb[kStages][kGroup];  // source texels of kStages groups (SC 4: whole words)
-  int cinb[2][kGroup];            // carry entries of this group and the next (lane 0; 0 elsewhere)
-  int pa, wa, wb;           // error of the texel at hand (carry aside); down-going x-1, x
+  int cinb[kStages][kGroup];      // carry entries of kStages groups (lane 0; 0 elsewhere)
+  int e7p;                  // 7/16 share of the previous texel
+  int dq;                   // complete down-going error from the row above for x
+  int wa, wb;               // down-going errors of this row for x-1, x
   int q[kGroup];            // quantised values of the group
   bool pairs;               // 8-byte source loads (SC 4, every row start 8-byte aligned)
   bool words;               // 4-byte source loads (SC 4, 4-byte aligned source)
@@ -171,12 +178,16 @@ struct Chan {
       emit_lane = a.height - 1 - strip * kLanes;
       emit_err = ((a.height - 1) & 1) == 0;
     }
-    pa = wa = wb = 0;
+    e7p = dq = wa = wb = 0;
 #pragma unroll
-    for (int k = 0; k < kGroup; ++k) cinb[0][k] = cinb[1][k] = 0;
+    for (int st = 0; st < kStages; ++st)
 #pragma unroll
-    for (int st = 0; st + 1 < kStages; ++st) load_src(st, st);
-    load_cin(0, 0);
+      for (int k = 0; k < kGroup; ++k) cinb[st][k] = 0;
+#pragma unroll
+    for (int st = 0; st + 1 < kStages; ++st) {
+      load_src(st, st);
+      load_cin(st, st);
+    }
   }
 
   // Source texels of group g into stage st.  The loads are unconditional (x
@@ -184,7 +195,7 @@ struct Chan {
   // branches around them: a texel outside the image only feeds a step that
   // does nothing.
   __device__ __forceinline__ void load_src(int st, int g) {
-    const int x0 = g * kGroup - 2 * lane;
+    const int x0 = g * kGroup - kLag * lane;
     if (pairs) {
 #pragma unroll
       for (int h = 0; h < kGroup / 2; ++h) {
@@ -240,24 +251,25 @@ struct Chan {
   }
 
   // Makes sure group g's carry words (stage CS) are written, then strips their
-  // tags (and zeroes them for every lane but 0, and past the row's end).  A group that is not there
-  // yet means the prefetch of the next group is stale as well, so the wait
-  // runs until the producer is two groups further on and then reloads both
-  // stages: that lag keeps later prefetches (issued a group ahead) from
-  // coming back empty.  The branch is warp-uniform.
+  // tags (and zeroes them for every lane but 0, and past the row's end).  A
+  // group that is not there yet means the prefetches of the next groups are
+  // stale as well, so the wait runs until the producer is kStages-1 groups
+  // further on and then reloads every stage: that lag keeps later prefetches
+  // (issued kStages-1 groups ahead) from coming back empty.  The branch is
+  // warp-uniform.
   template <int CS>
   __device__ __forceinline__ void take_cin(int g) {
     if (!has_in) return;
     const int x0 = g * kGroup;
     if (x0 < w && !cin_ready(CS, g)) {
-      const int* pw = cin + min(x0 + 3 * kGroup - 1, w - 1);  // last entry of group g+2
+      const int* pw = cin + min(x0 + kStages * kGroup - 1, w - 1);  // last entry of group g+kStages-1
       int spins = 0;
       while (ld_poll(pw) == 0 && ++spins < kSpinLimit)
         if ((spins & 255) == 0 && ld_poll(error)) break;
       spins = 0;
       do {
-        load_cin(CS, g);
-        load_cin(CS ^ 1, g + 1);
+#pragma unroll
+        for (int i = 0; i < kStages; ++i) load_cin((CS + i) % kStages, g + i);
       } while (!cin_ready(CS, g) && ++spins < 64 && !ld_poll(error));
       if (!cin_ready(CS, g) && lane == 0) atomicExch(error, 1);
     }
@@ -270,25 +282,26 @@ struct Chan {
   // values land in q[].
   template <int ST>
   __device__ __forceinline__ void steps(int g) {
-    constexpr int CS = ST & 1;
     load_src((ST + kStages - 1) % kStages, g + kStages - 1);
-    load_cin(CS ^ 1, g + 1);
-    take_cin<CS>(g);
-    const int x0 = g * kGroup - 2 * lane;
+    load_cin((ST + kStages - 1) % kStages, g + kStages - 1);
+    take_cin<ST>(g);
+    const int x0 = g * kGroup - kLag * lane;
     int ev[kGroup];
 #pragma unroll
     for (int k = 0; k < kGroup; ++k) {
       const int x = x0 + k;
       const bool act = row_ok && unsigned(x) < unsigned(w);
-      const int ein = pa + cinb[CS][k];
+      const int ein = e7p + dq + cinb[ST][k];
       const FsOut f = fs_step<BIT1>(widen12(src_byte(inb[ST][k])) + ein, act, qt);
       q[k] = f.q;
       // the entry for x-1 is complete; x and x+1 move up the window
       const int down = wa + f.e3;
       wa = wb + f.e5;
       wb = f.e1;
+      // the lane above is at x + 2: its complete entry is for x + 1
       const int up = __shfl_up_sync(0xffffffffu, down, 1);
-      pa = f.e7 + (lane ? up : 0);
+      e7p = f.e7;
+      dq = lane ? up : 0;
       ev[k] = emit_err ? ein : down;
     }
     // the emitting lane writes the group's completed entries: x-1 for each
@@ -318,14 +331,14 @@ __device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t
   const bool al_dst = a.dst8 && (((row_ok ? y : 0) & w & 1) == 0);
   uint8_t* ring8 = reinterpret_cast<uint8_t*>(ring[lane]);
   // the last lane reaches x = w (where it completes the entry for w-1) at
-  // step w + 2 * 31; whole windows so that every texel is written out
-  const int nsteps = w + 2 * (kLanes - 1) + 1;
+  // step w + kLag * 31; whole windows so that every texel is written out
+  const int nsteps = w + kLag * (kLanes - 1) + 1;
   const int ngroups = (nsteps + kWindow - 1) / kWindow * (kWindow / kGroup);
 
   auto group = [&](auto stc, int g) {
     constexpr int ST = decltype(stc)::value;
     c.template steps<ST>(g);
-    const int x0 = g * kGroup - 2 * lane;
+    const int x0 = g * kGroup - kLag * lane;
 #pragma unroll
     for (int k = 0; k < kGroup; ++k) {
       const int pos = (x0 + k) & (kRing - 1);
@@ -333,10 +346,10 @@ __device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t
       if (SC == 4 && AP == 255 && ch == 0) ring8[pos * 4 + 3] = uint8_t(c.inb[ST][k] >> 24);
     }
     if ((g + 1) % (kWindow / kGroup) == 0) {
-      // window m holds each lane's texels [32m - 2r, 32m + 32 - 2r); the ring
-      // keeps two windows, so one barrier per window is enough
+      // window m holds each lane's texels [32m - kLag r, 32m + 32 - kLag r);
+      // the ring keeps two windows, so one barrier per window is enough
       asm volatile("bar.sync 1, 96;" ::: "memory");
-      const int xs = (g + 1) * kGroup - kWindow - 2 * lane;
+      const int xs = (g + 1) * kGroup - kWindow - kLag * lane;
       for (int j = ch; j < kWindow / 2; j += 3) {
         const int x = xs + 2 * j;
         if (!row_ok || x < 0 || x >= w) continue;
@@ -356,11 +369,10 @@ __device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t
     }
   };
   for (int g = 0; g < ngroups; g += kStages) {
-    static_assert(kStages == 4, "stage unroll");
+    static_assert(kStages == 3, "stage unroll");
     group(std::integral_constant<int, 0>(), g);
     if (g + 1 < ngroups) group(std::integral_constant<int, 1>(), g + 1);
     if (g + 2 < ngroups) group(std::integral_constant<int, 2>(), g + 2);
-    if (g + 3 < ngroups) group(std::integral_constant<int, 3>(), g + 3);
   }
 }
 
@@ -389,21 +401,20 @@ __global__ void __launch_bounds__(kAlphaWarps * kLanes, 1) k_fs_alpha(FsArgs a) 
   const int y = strip * kLanes + lane;
   const bool row_ok = y < a.height;
   uint8_t* d = reinterpret_cast<uint8_t*>(a.dst + size_t(row_ok ? y : 0) * w) + 3;
-  const int ngroups = (w + 2 * (kLanes - 1) + 1 + kGroup - 1) / kGroup;
+  const int ngroups = (w + kLag * (kLanes - 1) + 1 + kGroup - 1) / kGroup;
   auto group = [&](auto stc, int g) {
     constexpr int ST = decltype(stc)::value;
     c.template steps<ST>(g);
-    const int x0 = g * kGroup - 2 * lane;
+    const int x0 = g * kGroup - kLag * lane;
 #pragma unroll
     for (int k = 0; k < kGroup; ++k)
       if (row_ok && unsigned(x0 + k) < unsigned(w)) d[size_t(x0 + k) * 4] = uint8_t(c.q[k]);
   };
   for (int g = 0; g < ngroups; g += kStages) {
-    static_assert(kStages == 4, "stage unroll");
+    static_assert(kStages == 3, "stage unroll");
     group(std::integral_constant<int, 0>(), g);
     if (g + 1 < ngroups) group(std::integral_constant<int, 1>(), g + 1);
     if (g + 2 < ngroups) group(std::integral_constant<int, 2>(), g + 2);
-    if (g + 3 < ngroups) group(std::integral_constant<int, 3>(), g + 3);
   }
 }
 
