@@ -49,6 +49,17 @@ constexpr int kRing = 2 * kWindow;   // texels per row in the ring
 constexpr int kRingStride = kRing + 1;
 static_assert((kRingStride - kLag) % 2 == 1 && kLag % 2 == 0, "ring banks, texel pairs");
 constexpr int kAlphaWarps = 4;       // strips per CTA of the alpha pass
+
+// How a warp fetches its source texels: RGBA8 rows read with asynchronous
+// copies into shared memory (8-byte pairs when every row start is 8-byte
+// aligned, else 4-byte words), or (RGB8, unaligned RGBA8) byte loads into
+// registers.  Shared memory per warp: kStages slots of kSlotWords words per
+// lane (12, so that four-word reads of eight lanes hit distinct banks).
+enum LoadMode { kLoadPairs, kLoadWords, kLoadBytes };
+constexpr int kSlotWords = 12;
+constexpr int kStageWords = kLanes * kSlotWords;
+constexpr int kWarpStageWords = kStages * kStageWords;
+static_assert(kGroup == 8, "a slot holds one group");
 constexpr int kSpinLimit = 1 << 22;  // polls of one carry word
 constexpr int kTagBias = 0x40000000; // carry word = value + bias; 0 = not written
 
@@ -107,6 +118,20 @@ __device__ __forceinline__ void st_tagged_if(bool on, int* p, int v) {
       "r"(v + kTagBias), "r"(int(on)));
 }
 
+__device__ __forceinline__ void cp_async(uint32_t* sdst, const uint8_t* gsrc, int bytes8) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(sdst));
+  const size_t g = __cvta_generic_to_global(gsrc);
+  if (bytes8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(g) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(g) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ int ld_poll(const int* p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -128,8 +153,8 @@ struct FsArgs {
 };
 
 // One channel of one strip, one lane per row, reading source byte `srcb`
-// (3 for alpha) of SC-byte texels.
-template <bool BIT1, int SC>
+// (3 for alpha) of SC-byte texels, fetched as LM says.
+template <bool BIT1, int SC, int LM>
 struct Chan {
   Quant qt;
   int srcb;
@@ -143,17 +168,17 @@ struct Chan {
   bool emit_err;           // write the texel's own error at x (red leftover of an even last row)
   int* error;
 
-  uint32_t inb[kStages][kGroup];  // source texels of kStages groups (SC 4: whole words)
+  uint32_t* slot;                 // this lane's stage-0 slot (asynchronous copies)
+  uint32_t inb[LM == kLoadBytes ? kStages : 1][kGroup];  // source texels of kStages groups (byte loads)
+  uint32_t cur[kGroup];           // source texels of the group at hand (SC 4: whole words)
   int cinb[kStages][kGroup];      // carry entries of kStages groups (lane 0; 0 elsewhere)
   int e7p;                  // 7/16 share of the previous texel
   int dq;                   // complete down-going error from the row above for x
   int wa, wb;               // down-going errors of this row for x-1, x
   int q[kGroup];            // quantised values of the group
-  bool pairs;               // 8-byte source loads (SC 4, every row start 8-byte aligned)
-  bool words;               // 4-byte source loads (SC 4, 4-byte aligned source)
 
   __device__ __forceinline__ void setup(const FsArgs& a, int strip, int ch, int nch, bool red_leftover, Quant q,
-                                        int sb) {
+                                        int sb, uint32_t* stage_buf) {
     qt = q;
     srcb = sb;
     w = a.width;
@@ -163,8 +188,7 @@ struct Chan {
     const int y = strip * kLanes + lane;
     row_ok = y < a.height;
     srow = a.src + size_t(row_ok ? y : 0) * w * SC;
-    words = SC == 4 && (reinterpret_cast<uintptr_t>(a.src) & 3) == 0;
-    pairs = words && a.src8 && (w & 1) == 0;
+    slot = stage_buf + lane * kSlotWords;
     has_in = strip > 0 || a.seeded;
     cin = a.carry + (size_t(strip) * nch + ch) * a.wpad;
     emit = nullptr;
@@ -190,26 +214,22 @@ struct Chan {
     }
   }
 
-  // Source texels of group g into stage st.  The loads are unconditional (x
-  // clamped into the row; rows past the image read row 0) so that no lane
+  // Source texels of group g into stage st.  The fetches are unconditional
+  // (x clamped into the row; rows past the image read row 0) so that no lane
   // branches around them: a texel outside the image only feeds a step that
-  // does nothing.
+  // does nothing.  Asynchronous copies form one commit group per group.
   __device__ __forceinline__ void load_src(int st, int g) {
     const int x0 = g * kGroup - kLag * lane;
-    if (pairs) {
+    if (LM == kLoadPairs) {
 #pragma unroll
-      for (int h = 0; h < kGroup / 2; ++h) {
-        const int x = min(max(x0 + 2 * h, 0), w - 2);
-        const uint2 p = __ldg(reinterpret_cast<const uint2*>(srow + size_t(x) * 4));
-        inb[st][2 * h] = p.x;
-        inb[st][2 * h + 1] = p.y;
-      }
-    } else if (words) {
+      for (int h = 0; h < kGroup / 2; ++h)
+        cp_async(slot + st * kStageWords + 2 * h, srow + size_t(min(max(x0 + 2 * h, 0), w - 2)) * 4, 1);
+      cp_async_commit();
+    } else if (LM == kLoadWords) {
 #pragma unroll
-      for (int k = 0; k < kGroup; ++k) {
-        const int x = min(max(x0 + k, 0), w - 1);
-        inb[st][k] = __ldg(reinterpret_cast<const uint32_t*>(srow + size_t(x) * 4));
-      }
+      for (int k = 0; k < kGroup; ++k)
+        cp_async(slot + st * kStageWords + k, srow + size_t(min(max(x0 + k, 0), w - 1)) * 4, 0);
+      cp_async_commit();
     } else if (SC == 4) {
 #pragma unroll
       for (int k = 0; k < kGroup; ++k) {
@@ -285,6 +305,17 @@ struct Chan {
     load_src((ST + kStages - 1) % kStages, g + kStages - 1);
     load_cin((ST + kStages - 1) % kStages, g + kStages - 1);
     take_cin<ST>(g);
+    if (LM == kLoadBytes) {
+#pragma unroll
+      for (int k = 0; k < kGroup; ++k) cur[k] = inb[ST][k];
+    } else {
+      // this group's copies are done once at most the two later ones are pending
+      cp_async_wait<kStages - 1>();
+      const uint4 lo = *reinterpret_cast<const uint4*>(slot + ST * kStageWords);
+      const uint4 hi = *reinterpret_cast<const uint4*>(slot + ST * kStageWords + 4);
+      cur[0] = lo.x, cur[1] = lo.y, cur[2] = lo.z, cur[3] = lo.w;
+      cur[4] = hi.x, cur[5] = hi.y, cur[6] = hi.z, cur[7] = hi.w;
+    }
     const int x0 = g * kGroup - kLag * lane;
     int ev[kGroup];
 #pragma unroll
@@ -292,7 +323,7 @@ struct Chan {
       const int x = x0 + k;
       const bool act = row_ok && unsigned(x) < unsigned(w);
       const int ein = e7p + dq + cinb[ST][k];
-      const FsOut f = fs_step<BIT1>(widen12(src_byte(inb[ST][k])) + ein, act, qt);
+      const FsOut f = fs_step<BIT1>(widen12(src_byte(cur[k])) + ein, act, qt);
       q[k] = f.q;
       // the entry for x-1 is complete; x and x+1 move up the window
       const int down = wa + f.e3;
@@ -318,11 +349,12 @@ struct Chan {
 // Colour pass: one CTA per strip, warp c runs channel c.  AP is the alpha
 // byte: for 3-component input the constant (1, 15 or 255); for 4 components
 // 255 copies the source alpha (8-bit alpha) and 0 leaves 0 for the alpha pass.
-template <int SC, int AP>
-__device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t (*ring)[kRingStride], int ch) {
+template <int SC, int AP, int LM>
+__device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t (*ring)[kRingStride],
+                                            uint32_t* stage_buf, int ch) {
   const Quant qt = ch == 1 ? Quant{2, 63, loop_mul(63)} : Quant{3, 31, loop_mul(31)};
-  Chan<false, SC> c;
-  c.setup(a, strip, ch, 3, ch == 0 && a.leftover != nullptr, qt, ch);
+  Chan<false, SC, LM> c;
+  c.setup(a, strip, ch, 3, ch == 0 && a.leftover != nullptr, qt, ch, stage_buf);
   const int lane = c.lane;
   const int w = a.width;
   const int y = strip * kLanes + lane;
@@ -343,7 +375,7 @@ __device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t
     for (int k = 0; k < kGroup; ++k) {
       const int pos = (x0 + k) & (kRing - 1);
       ring8[pos * 4 + ch] = uint8_t(c.q[k]);
-      if (SC == 4 && AP == 255 && ch == 0) ring8[pos * 4 + 3] = uint8_t(c.inb[ST][k] >> 24);
+      if (SC == 4 && AP == 255 && ch == 0) ring8[pos * 4 + 3] = uint8_t(c.cur[k] >> 24);
     }
     if ((g + 1) % (kWindow / kGroup) == 0) {
       // window m holds each lane's texels [32m - kLag r, 32m + 32 - kLag r);
@@ -374,28 +406,33 @@ __device__ __forceinline__ void colour_warp(const FsArgs& a, int strip, uint32_t
     if (g + 1 < ngroups) group(std::integral_constant<int, 1>(), g + 1);
     if (g + 2 < ngroups) group(std::integral_constant<int, 2>(), g + 2);
   }
+  if (LM != kLoadBytes) asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
-template <int SC, int AP>
+template <int SC, int AP, int LM>
 __global__ void __launch_bounds__(3 * kLanes, 1) k_fs_colour(FsArgs a) {
   __shared__ uint32_t ring[kLanes][kRingStride];
+  __shared__ __align__(16) uint32_t stage[LM == kLoadBytes ? 4 : 3 * kWarpStageWords];
   __shared__ int s_strip;
   if (threadIdx.x == 0) s_strip = int(atomicAdd(a.ticket, 1u));
   __syncthreads();
   const int strip = s_strip;
   if (strip >= a.nstrips) return;
-  colour_warp<SC, AP>(a, strip, ring, threadIdx.x >> 5);
+  const int warp = threadIdx.x >> 5;
+  colour_warp<SC, AP, LM>(a, strip, ring, stage + (LM == kLoadBytes ? 0 : warp * kWarpStageWords), warp);
 }
 
 // Alpha pass: one warp per strip, writing byte 3 of each texel.
-template <int AB>
+template <int AB, int LM>
 __global__ void __launch_bounds__(kAlphaWarps * kLanes, 1) k_fs_alpha(FsArgs a) {
+  __shared__ __align__(16) uint32_t stage[LM == kLoadBytes ? 4 : kAlphaWarps * kWarpStageWords];
   int strip = 0;
   if ((threadIdx.x & 31) == 0) strip = int(atomicAdd(a.ticket, 1u));
   strip = __shfl_sync(0xffffffffu, strip, 0);
   if (strip >= a.nstrips) return;
-  Chan<AB == 1, 4> c;
-  c.setup(a, strip, 0, 1, false, Quant{4, 15, loop_mul(15)}, 3);
+  Chan<AB == 1, 4, LM> c;
+  c.setup(a, strip, 0, 1, false, Quant{4, 15, loop_mul(15)}, 3,
+          stage + (LM == kLoadBytes ? 0 : (threadIdx.x >> 5) * kWarpStageWords));
   const int lane = c.lane;
   const int w = a.width;
   const int y = strip * kLanes + lane;
@@ -416,6 +453,7 @@ __global__ void __launch_bounds__(kAlphaWarps * kLanes, 1) k_fs_alpha(FsArgs a) 
     if (g + 1 < ngroups) group(std::integral_constant<int, 1>(), g + 1);
     if (g + 2 < ngroups) group(std::integral_constant<int, 2>(), g + 2);
   }
+  if (LM != kLoadBytes) asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 struct FsLayout {
@@ -468,15 +506,26 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const unsigned grid = unsigned(l.nstrips);
   const unsigned block = 3 * kLanes;
+  const uintptr_t sp = reinterpret_cast<uintptr_t>(d.src);
+  const int lm = d.srccomps == 4 && (sp & 7) == 0 && (w & 1) == 0 ? kLoadPairs
+                 : d.srccomps == 4 && (sp & 3) == 0              ? kLoadWords
+                                                                  : kLoadBytes;
   count_launches(1);
   if (d.srccomps == 3) {
-    if (d.alphabits == 1) k_fs_colour<3, 1><<<grid, block, 0, s>>>(a);
-    else if (d.alphabits == 4) k_fs_colour<3, 15><<<grid, block, 0, s>>>(a);
-    else k_fs_colour<3, 255><<<grid, block, 0, s>>>(a);
+    if (d.alphabits == 1) k_fs_colour<3, 1, kLoadBytes><<<grid, block, 0, s>>>(a);
+    else if (d.alphabits == 4) k_fs_colour<3, 15, kLoadBytes><<<grid, block, 0, s>>>(a);
+    else k_fs_colour<3, 255, kLoadBytes><<<grid, block, 0, s>>>(a);
     return cudaGetLastError();
   }
-  if (alpha_pass) k_fs_colour<4, 0><<<grid, block, 0, s>>>(a);
-  else k_fs_colour<4, 255><<<grid, block, 0, s>>>(a);
+  if (alpha_pass) {
+    if (lm == kLoadPairs) k_fs_colour<4, 0, kLoadPairs><<<grid, block, 0, s>>>(a);
+    else if (lm == kLoadWords) k_fs_colour<4, 0, kLoadWords><<<grid, block, 0, s>>>(a);
+    else k_fs_colour<4, 0, kLoadBytes><<<grid, block, 0, s>>>(a);
+  } else {
+    if (lm == kLoadPairs) k_fs_colour<4, 255, kLoadPairs><<<grid, block, 0, s>>>(a);
+    else if (lm == kLoadWords) k_fs_colour<4, 255, kLoadWords><<<grid, block, 0, s>>>(a);
+    else k_fs_colour<4, 255, kLoadBytes><<<grid, block, 0, s>>>(a);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess || !alpha_pass) return e;
   // alpha pass, seeded with the red leftover row
@@ -487,8 +536,16 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   b.ticket = tickets + 1;
   const unsigned agrid = (unsigned(l.nstrips) + kAlphaWarps - 1) / kAlphaWarps;
   count_launches(1);
-  if (d.alphabits == 1) k_fs_alpha<1><<<agrid, kAlphaWarps * kLanes, 0, s>>>(b);
-  else k_fs_alpha<4><<<agrid, kAlphaWarps * kLanes, 0, s>>>(b);
+  const unsigned ablock = kAlphaWarps * kLanes;
+  if (d.alphabits == 1) {
+    if (lm == kLoadPairs) k_fs_alpha<1, kLoadPairs><<<agrid, ablock, 0, s>>>(b);
+    else if (lm == kLoadWords) k_fs_alpha<1, kLoadWords><<<agrid, ablock, 0, s>>>(b);
+    else k_fs_alpha<1, kLoadBytes><<<agrid, ablock, 0, s>>>(b);
+  } else {
+    if (lm == kLoadPairs) k_fs_alpha<4, kLoadPairs><<<agrid, ablock, 0, s>>>(b);
+    else if (lm == kLoadWords) k_fs_alpha<4, kLoadWords><<<agrid, ablock, 0, s>>>(b);
+    else k_fs_alpha<4, kLoadBytes><<<agrid, ablock, 0, s>>>(b);
+  }
   return cudaGetLastError();
 }
 

@@ -135,6 +135,24 @@ def test_fs_strip_edges(lib, oracle):
             assert np.array_equal(a, b), (w, h, sc, ab)
 
 
+def test_fs_unaligned_device_source(lib, oracle):
+    """Floyd-Steinberg from device sources 1, 2 and 4 bytes past an aligned
+    address (byte loads, byte loads, 4-byte copies) and at the aligned one."""
+    import torch
+    rng = np.random.default_rng(78)
+    for w, h in ((70, 45), (33, 40)):
+        img = cases.image(rng, w, h, 4, 0)
+        for fmt in (0x83F1, 0x83F3):
+            want = oracle.compress(4, w, h, img, fmt, 2, 5, -1, 1)
+            for off in (0, 1, 2, 4):
+                buf = torch.zeros(off + img.size, dtype=torch.uint8, device="cuda")
+                buf[off:] = torch.from_numpy(img).cuda()
+                d_dst = torch.zeros(s2.compressed_size(w, h, fmt), dtype=torch.uint8, device="cuda")
+                s2.gpu_compress(4, w, h, buf.data_ptr() + off, fmt, d_dst, opt=s2.options(2, 5, -1, 1))
+                torch.cuda.synchronize()
+                assert np.array_equal(d_dst.cpu().numpy(), want), (w, h, hex(fmt), off)
+
+
 def test_row_stride(lib, oracle):
     rng = np.random.default_rng(5)
     for fmt in cases.FORMATS:
