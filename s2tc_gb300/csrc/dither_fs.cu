@@ -203,7 +203,8 @@ struct FsArgs {
   int width, height;
   int nstrips;
   int wpad;             // carry row length, width rounded up to a whole group
-  int* carry;           // nstrips * channels rows; strip s, channel c reads row s * channels + c
+  int* carry;           // carry rows between clusters: the first strip of cluster k, channel c,
+                        // reads row k * channels + c (row 0: the alpha pass's seed, else unused)
   int* leftover;        // colour pass followed by an alpha pass: the alpha pass's first carry row
   int seeded;           // alpha pass: strip 0 reads its carry row (the red leftover)
   int dst8;             // 8-byte aligned destination
@@ -271,7 +272,7 @@ struct Chan {
     srow = a.src + size_t(row_ok ? y : 0) * w * SC;
     slot = stage_buf + lane * kSlotWords;
     in_mode = strip == 0 && !a.seeded ? kInNone : rank > 0 ? kInRing : kInRow;
-    cin = a.carry + (size_t(strip) * NCH + ch) * a.wpad;
+    cin = a.carry + (size_t(strip / kCluster) * NCH + ch) * a.wpad;
     rin = cs.ring[ch];
     prog_up = rank > 0 ? map_rank(&cs.prog[ch], rank - 1) : 0;
     out_mode = kOutNone;
@@ -287,7 +288,7 @@ struct Chan {
         rout = map_rank(&cs.ring[ch][0], rank + 1);
       } else {
         out_mode = kOutRow;
-        emit = a.carry + (size_t(strip + 1) * NCH + ch) * a.wpad;
+        emit = a.carry + (size_t((strip + 1) / kCluster) * NCH + ch) * a.wpad;
       }
     } else if (red_leftover) {
       out_mode = kOutRow;
@@ -610,16 +611,19 @@ __global__ void __launch_bounds__(kLanes, 1) k_fs_alpha(FsArgs a) {
 }
 
 struct FsLayout {
-  int nstrips, wpad;
+  int nstrips, nrows, wpad;
   size_t rgb_bytes, alpha_bytes;
 };
 
+// One carry row per channel and cluster (the strips inside a cluster hand
+// their carries over in shared memory).
 FsLayout fs_layout(int width, int height) {
   FsLayout l;
   l.nstrips = (height + kLanes - 1) / kLanes;
+  l.nrows = (l.nstrips + kCluster - 1) / kCluster;
   l.wpad = ((width + kGroup - 1) / kGroup) * kGroup;
-  l.rgb_bytes = size_t(l.nstrips) * 3 * l.wpad * sizeof(int);
-  l.alpha_bytes = size_t(l.nstrips) * l.wpad * sizeof(int);
+  l.rgb_bytes = size_t(l.nrows) * 3 * l.wpad * sizeof(int);
+  l.alpha_bytes = size_t(l.nrows) * l.wpad * sizeof(int);
   return l;
 }
 
@@ -667,9 +671,9 @@ cudaError_t launch_dither_fs(DitherArgs d, uint8_t* scratch, cudaStream_t s) {
   a.dst8 = (reinterpret_cast<uintptr_t>(d.dst) & 7) == 0;
   a.ticket = tickets;
   a.error = d.error;
-  // the carry rows of strip 0 are never read in the colour pass
+  // the colour pass's row 0 is never read (the first strip has no input)
   const size_t skip = size_t(l.wpad) * 3 * sizeof(int);
-  cudaError_t e = cudaMemsetAsync(scratch + skip, 0, l.rgb_bytes - skip, s);
+  cudaError_t e = l.rgb_bytes > skip ? cudaMemsetAsync(scratch + skip, 0, l.rgb_bytes - skip, s) : cudaSuccess;
   if (e == cudaSuccess && alpha_pass) e = cudaMemsetAsync(alpha_carry, 0, l.alpha_bytes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(tickets, 0, 2 * sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;

@@ -22,6 +22,8 @@ def test_noalloc_matches_gpu_compress_twice(lib):
         (workloads.value_noise_rgba(11, 2048, 2048), 2048, 2048, 0x83F3, s2.options(1, s2.SRGB_MIXED, 0, 2)),
         # 1000x613 RGBA -> DXT1, WAVG quick selection, ALWAYS, Floyd-Steinberg
         (workloads.plain_rgba(12, 1000, 613), 1000, 613, 0x83F1, s2.options(2, s2.WAVG, -1, 1)),
+        # 2048x2048 RGBA -> DXT1, Floyd-Steinberg with its alpha pass (the size limit)
+        (workloads.plain_rgba(13, 2048, 2048), 2048, 2048, 0x83F1, s2.options(2, s2.WAVG, -1, 1)),
     ]
     for img, w, h, fmt, opt in calls:
         d_src = torch.from_numpy(img.reshape(-1).copy()).cuda()
