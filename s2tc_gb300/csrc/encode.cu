@@ -47,7 +47,8 @@ constexpr bool kSymmetric = kMetric != CD_SRGB;
 // Per-thread scratch columns in shared memory (index [k][thread]).
 struct Scratch16 {
   P pin[16][kThreadsPerCta];
-  int ain[16][kThreadsPerCta];
+  int ain[16][kThreadsPerCta];   // distinct alpha values of the block, ascending
+  int ast[16][kThreadsPerCta];   // where each value's run starts in the sorted alphas
 };
 
 // Pick the pair the reference keeps: pairs in (i, j) lexicographic order,
@@ -104,31 +105,63 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, uint32_t mask, Scratch
 // reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) for n = m = 16
 // on the alpha values.  Each input's cost is the smallest squared distance to
 // the pair or to the fixed values 0 and 255; the minimum of squares of
-// non-negative numbers is the square of their minimum, so the search runs on
-// absolute differences.  Its conditional write-back into c[0]/c[1] reads the
-// candidates before changing them, so the result is simply the winning pair.
+// non-negative numbers is the square of their minimum.  Its conditional
+// write-back into c[0]/c[1] reads the candidates before changing them, so the
+// result is simply the winning pair.
+//
+// Every input k adds min(d(i,k), d(j,k)) to the sum of pair (i, j), and inputs
+// with equal alpha add equal amounts, so the loop runs over the block's
+// distinct alpha values (2.6 per block on a typical texture with alpha) and
+// adds each one's contribution times its count: the same integer sums, in
+// fewer passes over the 120 pairs.
 __device__ __forceinline__ void reduce16_alpha(const int* ain, Scratch16& sc, int& besti, int& bestj) {
   const int t = threadIdx.x;
+  // distinct values and their counts: a bitonic sort, then the runs
+  int v[16];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) sc.ain[i][t] = ain[i];
+  for (int i = 0; i < 16; ++i) v[i] = ain[i];
+#pragma unroll
+  for (int k = 2; k <= 16; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const int lo = min(v[i], v[l]), hi = max(v[i], v[l]);
+          const bool up = (i & k) == 0;
+          v[i] = up ? lo : hi;
+          v[l] = up ? hi : lo;
+        }
+      }
+  int nd = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    if (i == 0 || v[i] != v[i - 1]) {
+      sc.ain[nd][t] = v[i];
+      sc.ast[nd][t] = i;
+      ++nd;
+    }
+  }
   int32_t S[120];
 #pragma unroll
   for (int p = 0; p < 120; ++p) S[p] = 0;
 #pragma unroll 1
-  for (int k = 0; k < 16; ++k) {
-    const int ak = sc.ain[k][t];
+  for (int d = 0; d < nd; ++d) {
+    const int ak = sc.ain[d][t];
+    const int wk = (d + 1 < nd ? sc.ast[d + 1][t] : 16) - sc.ast[d][t];
     const int fk = min(ak, 255 - ak);
     int col[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) col[i] = min(abs(ain[i] - ak), fk);
+    for (int i = 0; i < 16; ++i) {
+      const int c = min(abs(ain[i] - ak), fk);
+      col[i] = c * c;
+    }
     int p = 0;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
 #pragma unroll
-      for (int j = i + 1; j < 16; ++j, ++p) {
-        const int v = min(col[i], col[j]);
-        S[p] += v * v;
-      }
+      for (int j = i + 1; j < 16; ++j, ++p) S[p] += wk * min(col[i], col[j]);
   }
   pick_pair(S, 0xFFFFu, besti, bestj);
 }
