@@ -48,8 +48,26 @@ constexpr bool kSymmetric = kMetric != CD_SRGB;
 struct Scratch16 {
   P pin[16][kThreadsPerCta];
   int ain[16][kThreadsPerCta];   // distinct alpha values of the block, ascending
-  int ast[16][kThreadsPerCta];   // where each value's run starts in the sorted alphas
+  int ast[16][kThreadsPerCta];   // where each value's run starts in the sorted values
 };
+
+// Sorts 16 values ascending (bitonic network, unrolled).
+__device__ __forceinline__ void sort16(int* v) {
+#pragma unroll
+  for (int k = 2; k <= 16; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const int lo = min(v[i], v[l]), hi = max(v[i], v[l]);
+          const bool up = (i & k) == 0;
+          v[i] = up ? lo : hi;
+          v[l] = up ? hi : lo;
+        }
+      }
+}
 
 // Pick the pair the reference keeps: pairs in (i, j) lexicographic order,
 // taken when `bestsum < 0 || sum < bestsum` (s2tc_algorithm.cpp:404-409).
@@ -116,24 +134,11 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, uint32_t mask, Scratch
 // fewer passes over the 120 pairs.
 __device__ __forceinline__ void reduce16_alpha(const int* ain, Scratch16& sc, int& besti, int& bestj) {
   const int t = threadIdx.x;
-  // distinct values and their counts: a bitonic sort, then the runs
+  // distinct values and their counts: a sort, then the runs
   int v[16];
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = ain[i];
-#pragma unroll
-  for (int k = 2; k <= 16; k <<= 1)
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int l = i ^ j;
-        if (l > i) {
-          const int lo = min(v[i], v[l]), hi = max(v[i], v[l]);
-          const bool up = (i & k) == 0;
-          v[i] = up ? lo : hi;
-          v[l] = up ? hi : lo;
-        }
-      }
+  sort16(v);
   int nd = 0;
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
