@@ -302,6 +302,7 @@ struct TileSmem {
   uint32_t tab3[32], tab2[64], tab4[16];
   uint32_t wagg[kWarps][kRecWords];  // warps' inclusive records
   uint32_t wstart[kWarps];           // warps' start states
+  uint32_t lb[32][kRecWords + 1];     // look-back window: aggregates of 32 earlier tiles
   uint32_t carry;
   alignas(8) unsigned long long mbar;  // completion of the tile's bulk copy
 };
@@ -429,43 +430,71 @@ constexpr int kSpinLimit = 1 << 22;
 
 // The state at the start of tile g of an image whose tile within the image
 // is `lt`, given the tile's aggregate; publishes the tile's own records.
+// The tile's start state, by one warp.  The tile publishes its aggregate,
+// then its lanes read the status words of the 32 tiles before it at once: the
+// nearest one that has published its end state ("inclusive") ends the walk,
+// and the aggregates of the tiles between it and this one are applied to that
+// state in order.  A window without any end state (only aggregates) is
+// composed into one record and the walk moves 32 tiles further back.  The
+// image's first tile publishes its end state without looking back, so the
+// walk never leaves the image.  Finally the tile publishes its own end state.
 template <int AK>
-__device__ uint32_t look_back(const DitherWork& w, long long g, long long lt, const Rec& agg) {
+__device__ uint32_t look_back(const DitherWork& w, long long g, long long lt, const Rec& agg, TileSmem& sm) {
+  const int lane = threadIdx.x & 31;
   Status st(w.status[g]);
   if (lt == 0) {
     const uint32_t carry = initial_state<AK>();
-    st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+    if (lane == 0) st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
     return carry;
   }
-  uint32_t* gagg = reinterpret_cast<uint32_t*>(w.aggs + g * kRec);
-  rec_store(gagg, agg);
-  st.store(kAggReady, cuda::memory_order_release);
-  // acc: state at the end of tile k -> state at the start of this tile; the
-  // image's first tile always publishes its inclusive state, so the walk
-  // never leaves the image
-  Rec acc;
+  if (lane == 0) {
+    rec_store(reinterpret_cast<uint32_t*>(w.aggs + g * kRec), agg);
+    st.store(kAggReady, cuda::memory_order_release);
+  }
+  const long long first = g - lt;  // the image's first tile
+  Rec acc;                          // the tiles after the current window, up to g - 1 (lane 0)
   rec_identity<AK>(acc);
   uint32_t carry = initial_state<AK>();
-  for (long long k = g - 1;; --k) {
-    Status sk(w.status[k]);
-    unsigned long long v = sk.load(cuda::memory_order_acquire);
-    int spins = 0;
-    while ((v >> 32) == 0 && spins < kSpinLimit) {
-      __nanosleep(64);
+  for (long long top = g - 1;; top -= 32) {
+    const long long k = top - lane;
+    const bool valid = k >= first;
+    unsigned long long v = 0;
+    if (valid) {
+      Status sk(w.status[k]);
       v = sk.load(cuda::memory_order_acquire);
-      ++spins;
+      int spins = 0;
+      while ((v >> 32) == 0 && spins < kSpinLimit) {
+        __nanosleep(64);
+        v = sk.load(cuda::memory_order_acquire);
+        ++spins;
+      }
     }
-    if ((v >> 32) == 0) {
-      atomicExch(w.error, 1);
+    if (__any_sync(0xFFFFFFFFu, valid && (v >> 32) == 0)) {
+      if (lane == 0) atomicExch(w.error, 1);
       break;
     }
-    if ((v >> 32) == 2) {
-      carry = apply<AK>(acc, uint32_t(v));
+    const unsigned inc = __ballot_sync(0xFFFFFFFFu, valid && (v >> 32) == 2);
+    const int nagg = inc ? __ffs(int(inc)) - 1 : 32;  // lanes 0 .. nagg-1 hold aggregates
+    if (lane < nagg) rec_store(sm.lb[lane], rec_load_global(reinterpret_cast<const uint32_t*>(w.aggs + k * kRec)));
+    __syncwarp();
+    if (inc) {
+      uint32_t s = __shfl_sync(0xFFFFFFFFu, uint32_t(v), nagg);  // end state of tile top - nagg
+      if (lane == 0) {
+        for (int j = nagg - 1; j >= 0; --j) s = apply<AK>(rec_load(sm.lb[j]), s);
+        s = apply<AK>(acc, s);
+      }
+      carry = __shfl_sync(0xFFFFFFFFu, s, 0);
       break;
     }
-    acc = compose<AK>(rec_load_global(reinterpret_cast<const uint32_t*>(w.aggs + k * kRec)), acc);
+    if (lane == 0) {
+      // the window's tiles in order (top - 31 .. top), then the later ones
+      Rec win = rec_load(sm.lb[31]);
+      for (int j = 30; j >= 0; --j) win = compose<AK>(win, rec_load(sm.lb[j]));
+      acc = compose<AK>(win, acc);
+    }
+    __syncwarp();
   }
-  st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+  if (lane == 0) st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
   return carry;
 }
 
@@ -554,9 +583,7 @@ __device__ __forceinline__ void simple_tile(const DitherItem& it, long long lt, 
     for (int i = 0; i < 2; ++i) agg.g[i] = __shfl_sync(0xFFFFFFFFu, y.g[i], kWarps - 1);
 #pragma unroll
     for (int i = 0; i < 8; ++i) agg.a[i] = __shfl_sync(0xFFFFFFFFu, y.a[i], kWarps - 1);
-    uint32_t carry = 0;
-    if (lane == 0) carry = look_back<AK>(w, g, lt, agg);
-    carry = __shfl_sync(0xFFFFFFFFu, carry, 0);
+    const uint32_t carry = look_back<AK>(w, g, lt, agg, sm);
     // start of warp l = end of warp l-1
     const uint32_t end = apply<AK>(y, carry);
     const uint32_t start = __shfl_up_sync(0xFFFFFFFFu, end, 1);
