@@ -356,8 +356,13 @@ bool host_pinned(const void* p) {
 // back (per range when `dest` is pinned, else at the end).  Same kernels and
 // bytes as the unpipelined path.  Returns false when the image does not
 // qualify (the caller then takes that path).
+// Ranges: about kPipeTargetRanges of them, at least kPipeRangeTiles tiles
+// each.  Every range costs a dozen stream operations on the host (about 40 µs
+// on the GB300 host), so more ranges starve the GPU; fewer leave more of the
+// first upload and the last encode outside the overlap.
 constexpr long long kPipeMinTexels = 1ll << 22;
 constexpr long long kPipeRangeTiles = 128;
+constexpr long long kPipeTargetRanges = 8;
 
 bool compress_host_pipelined(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                              unsigned char* dest, long long diff, const s2tc_options& opt, bool* done) {
@@ -374,7 +379,7 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   const long long row_bytes = (long long)bw * bs;
   const long long tile = dither_tile_texels();
   const long long tiles = (npx + tile - 1) / tile;
-  const long long per_range = std::max(kPipeRangeTiles, (tiles + Context::kPipeRanges - 1) / Context::kPipeRanges);
+  const long long per_range = std::max(kPipeRangeTiles, (tiles + kPipeTargetRanges - 1) / kPipeTargetRanges);
   const int ranges = int((tiles + per_range - 1) / per_range);
   if (!c.src.reserve(size_t(npx) * sc + 16, "cudaMalloc(src)")) return true;
   if (!c.dst.reserve(size_t(row_bytes) * bh + 16, "cudaMalloc(dst)")) return true;
