@@ -36,7 +36,11 @@
 namespace s2tc {
 namespace {
 
-constexpr int kSlots = 4;                 // rounds in flight at most
+// Rounds in flight at most.  A round holds its slot from launch until the
+// scheduler sees its download done (upload, kernels, download and the retire
+// poll: a few hundred microseconds even for small requests), so under a steady
+// stream of small requests the slot count bounds the rounds per second.
+constexpr int kSlots = 16;
 constexpr int kMaxRoundRequests = 256;    // requests per round at most
 constexpr size_t kAlign = 256;
 
@@ -383,7 +387,11 @@ void scheduler(s2tc_server* sv) {
         free_slot->busy = true;
         sv->max_round = std::max(sv->max_round, int(free_slot->reqs.size()));
         ++sv->rounds;
+        // the round's requests and slot belong to the scheduler now: submitters
+        // need not wait while its stream operations are issued
+        lk.unlock();
         const int st = launch_round(sv, *free_slot);
+        lk.lock();
         if (st != S2TC_OK) {
           for (auto& r : free_slot->reqs) {
             r->status = -st;
