@@ -113,7 +113,7 @@ def test_every_mode_combination(lib, oracle, fmt):
 
 @pytest.mark.parametrize("dither", [0, 1, 2])
 def test_rgb565_image_many_tiles(lib, oracle, dither):
-    """Images that span many scan tiles / wavefront bands."""
+    """Images that span many scan tiles and Floyd-Steinberg strips and clusters."""
     rng = np.random.default_rng(40 + dither)
     for w, h in ((1000, 613), (3, 2000), (4099, 37), (257, 300)):
         for sc, ab in ((4, 1), (4, 4), (3, 8), (4, 8)):
