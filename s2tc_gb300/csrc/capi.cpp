@@ -91,7 +91,8 @@ struct Context {
   DevBuf mips, blocks;  // s2tc_compress_dds: every level's pixels and blocks
   DevBuf rnd_win;       // the rand() stream position for the device generator
   // pipelined tx_compress_dxtn: upload and download streams, per-range events
-  cudaStream_t copy_in = nullptr, copy_out = nullptr, encode_stream = nullptr;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, encode_stream[2] = {nullptr, nullptr};
+  cudaEvent_t pipe_first = nullptr;  // the first range's encode (it reads the carried endpoint)
   static constexpr int kPipeRanges = 64;
   cudaEvent_t pipe_in[kPipeRanges] = {}, pipe_mid[kPipeRanges] = {}, pipe_out[kPipeRanges] = {};
   bool pipe_ready = false;
@@ -99,7 +100,9 @@ struct Context {
     if (pipe_ready) return true;
     if (!cuda_ok(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !cuda_ok(cudaStreamCreateWithFlags(&encode_stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+        !cuda_ok(cudaStreamCreateWithFlags(&encode_stream[0], cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&encode_stream[1], cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaEventCreateWithFlags(&pipe_first, cudaEventDisableTiming), "cudaEventCreate"))
       return false;
     for (int i = 0; i < kPipeRanges; ++i)
       if (!cuda_ok(cudaEventCreateWithFlags(&pipe_in[i], cudaEventDisableTiming), "cudaEventCreate") ||
@@ -350,9 +353,9 @@ bool host_pinned(const void* p) {
 
 // tx_compress_dxtn on a large image, pipelined: the image goes up in ranges of
 // whole dither tiles on one copy stream; the dither stream scans each range
-// as it lands (the scan's look-back reaches into the ranges before it); an
-// encode stream encodes the block rows whose four texel rows are complete
-// while the next range is dithered; a second copy stream brings those rows
+// as it lands (the scan's look-back reaches into the ranges before it); two
+// encode streams, in turn, encode the block rows whose four texel rows are
+// complete while the next range is dithered; a second copy stream brings those rows
 // back (per range when `dest` is pinned, else at the end).  Same kernels and
 // bytes as the unpipelined path.  Returns false when the image does not
 // qualify (the caller then takes that path).
@@ -374,7 +377,7 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   if (per_block > 0 && !rand_usable()) return false;
   if (!c.init_pipe()) return false;
   *done = true;
-  cudaStream_t s = c.stream, se = c.encode_stream;
+  cudaStream_t s = c.stream;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
   const long long row_bytes = (long long)bw * bs;
   const long long tile = dither_tile_texels();
@@ -431,7 +434,7 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
     ea.prev_a1_dev = c.err.as<int>() + 2;
     ea.leftover_out = c.err.as<int>() + 2;
   }
-  int rows_done = 0;
+  int rows_done = 0, nenc = 0;
   for (int r = 0; r < ranges; ++r) {
     const long long t0 = r * per_range, t1 = std::min(tiles, t0 + per_range);
     const long long p0 = t0 * tile, p1 = std::min(npx, t1 * tile);
@@ -447,10 +450,19 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
     ea.by0 = rows_done;
     ea.nby = rows_ready - rows_done;
     ea.rnd = rnd ? rnd + (long long)rows_done * bw * per_block : nullptr;
+    // consecutive ranges alternate between two encode streams, so that one
+    // range's encode fills the last, partial wave of the one before
+    cudaStream_t se = c.encode_stream[nenc & 1];
     if (!cuda_ok(cudaEventRecord(c.pipe_mid[r], s), "cudaEventRecord") ||
-        !cuda_ok(cudaStreamWaitEvent(se, c.pipe_mid[r], 0), "cudaStreamWaitEvent") ||
-        !cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, se), "encode launch"))
+        !cuda_ok(cudaStreamWaitEvent(se, c.pipe_mid[r], 0), "cudaStreamWaitEvent"))
       return true;
+    // the last rows write the carried endpoint that the first rows read
+    if (rows_ready == bh && nenc > 0 && (nenc & 1) &&
+        !cuda_ok(cudaStreamWaitEvent(se, c.pipe_first, 0), "cudaStreamWaitEvent"))
+      return true;
+    if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, se), "encode launch")) return true;
+    if (nenc == 0 && !cuda_ok(cudaEventRecord(c.pipe_first, se), "cudaEventRecord")) return true;
+    ++nenc;
     if (pinned_out) {
       if (!cuda_ok(cudaEventRecord(c.pipe_out[r], se), "cudaEventRecord") ||
           !cuda_ok(cudaStreamWaitEvent(c.copy_out, c.pipe_out[r], 0), "cudaStreamWaitEvent") ||
@@ -462,10 +474,11 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
     }
     rows_done = rows_ready;
   }
-  // the compute stream joins the encode stream, then (unpinned output) downloads
-  if (!cuda_ok(cudaEventRecord(c.pipe_mid[0], se), "cudaEventRecord") ||
-      !cuda_ok(cudaStreamWaitEvent(s, c.pipe_mid[0], 0), "cudaStreamWaitEvent"))
-    return true;
+  // the compute stream joins the encode streams, then (unpinned output) downloads
+  for (int k = 0; k < 2; ++k)
+    if (!cuda_ok(cudaEventRecord(c.pipe_mid[k], c.encode_stream[k]), "cudaEventRecord") ||
+        !cuda_ok(cudaStreamWaitEvent(s, c.pipe_mid[k], 0), "cudaStreamWaitEvent"))
+      return true;
   if (!pinned_out &&
       !cuda_ok(cudaMemcpy2DAsync(dest, size_t(row_bytes + diff), d_dst, size_t(row_bytes), size_t(row_bytes),
                                  size_t(bh), cudaMemcpyDeviceToHost, s),
@@ -474,8 +487,7 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   if (!cuda_ok(cudaEventRecord(c.pipe_out[0], c.copy_out), "cudaEventRecord") ||
       !cuda_ok(cudaStreamWaitEvent(s, c.pipe_out[0], 0), "cudaStreamWaitEvent") ||
       !cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord"))
-    return true;
-  check_error_flag(c, s);
+    return true;  check_error_flag(c, s);
   return true;
 }
 
