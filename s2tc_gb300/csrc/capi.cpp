@@ -113,6 +113,7 @@ struct Context {
     return true;
   }
   PinnedBuf host_rnd, host_out;
+  PinnedBuf host_flag;  // where the timeout flag is read back to
 
   bool init() {
     if (ready) return true;
@@ -125,6 +126,7 @@ struct Context {
     if (!cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate")) return false;
     if (!cuda_ok(cudaEventCreateWithFlags(&arena_free, cudaEventDisableTiming), "cudaEventCreate")) return false;
     if (!err.reserve(sizeof(int) * 4, "cudaMalloc(error flag)")) return false;
+    if (!host_flag.reserve(sizeof(int), "cudaMallocHost(error flag)")) return false;
     if (!cuda_ok(cudaMemset(err.p, 0, sizeof(int) * 4), "cudaMemset")) return false;
     // err[2]: the carried alpha endpoint of tx_compress_dxtn calls (-1: none yet)
     if (!cuda_ok(cudaMemset(err.as<int>() + 2, 0xFF, sizeof(int)), "cudaMemset")) return false;
@@ -328,18 +330,29 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
   return ST_OK;
 }
 
-// Waits for `s`, then reads and clears the kernels' sticky timeout flag.
-int check_error_flag(Context& c, cudaStream_t s) {
-  int flag = 0;
-  if (!cuda_ok(cudaMemcpyAsync(&flag, c.err.p, sizeof(int), cudaMemcpyDeviceToHost, s), "error flag read"))
-    return ST_CUDA_ERROR;
-  if (!cuda_ok(cudaMemsetAsync(c.err.p, 0, sizeof(int), s), "cudaMemsetAsync")) return ST_CUDA_ERROR;
-  if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return ST_CUDA_ERROR;
+// Enqueues on `s` the read-back (into pinned memory) and the reset of the
+// kernels' sticky timeout flag.
+bool enqueue_flag(Context& c, cudaStream_t s) {
+  return cuda_ok(cudaMemcpyAsync(c.host_flag.p, c.err.p, sizeof(int), cudaMemcpyDeviceToHost, s), "error flag read") &&
+         cuda_ok(cudaMemsetAsync(c.err.p, 0, sizeof(int), s), "cudaMemsetAsync");
+}
+
+// The flag's verdict, once the stream that read it back has been waited for.
+int take_flag(Context& c) {
+  int& flag = *static_cast<int*>(c.host_flag.p);
   if (flag) {
+    flag = 0;
     set_error("a bounded wait in the dither scan gave up");
     return ST_TIMEOUT;
   }
   return ST_OK;
+}
+
+// Waits for `s`, then reads and clears the kernels' sticky timeout flag.
+int check_error_flag(Context& c, cudaStream_t s) {
+  if (!enqueue_flag(c, s)) return ST_CUDA_ERROR;
+  if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return ST_CUDA_ERROR;
+  return take_flag(c);
 }
 
 bool host_pinned(const void* p) {
@@ -487,7 +500,8 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   if (!cuda_ok(cudaEventRecord(c.pipe_out[0], c.copy_out), "cudaEventRecord") ||
       !cuda_ok(cudaStreamWaitEvent(s, c.pipe_out[0], 0), "cudaStreamWaitEvent") ||
       !cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord"))
-    return true;  check_error_flag(c, s);
+    return true;
+  check_error_flag(c, s);
   return true;
 }
 
@@ -517,7 +531,9 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
   if (compress_device_locked(c, sc, width, height, c.src.as<uint8_t>(), dxt, c.dst.as<uint8_t>(), (long long)row_bytes,
                              opt, nullptr, s, c.err.as<int>() + 2) != ST_OK)
     return;
-  if (check_error_flag(c, s) != ST_OK) return;
+  // the flag read goes ahead of the output download: one wait for both (a
+  // call whose bounded wait gave up reports it, its output is undefined)
+  if (!enqueue_flag(c, s)) return;
   // Output rows: packed, or dstRowStride apart (s2tc_libtxc_dxtn.cpp:243, 261, 279).
   const long long diff =
       dstRowStride >= width * (bs / 4) ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs / 4) : 0;
@@ -531,13 +547,13 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
     if (!c.host_out.reserve(row_bytes * bh, "cudaMallocHost(output)")) return;
     if (!cuda_ok(cudaMemcpyAsync(c.host_out.p, c.dst.p, row_bytes * bh, cudaMemcpyDeviceToHost, s), "output download"))
       return;
-    if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return;
+    if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize") || take_flag(c) != ST_OK) return;
     for (int r = 0; r < bh; ++r)
       std::memmove(dest + r * (long long)(row_bytes + diff), static_cast<unsigned char*>(c.host_out.p) + r * row_bytes,
                    row_bytes);
     return;
   }
-  cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  if (cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) take_flag(c);
 }
 
 
