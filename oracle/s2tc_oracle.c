@@ -34,6 +34,11 @@
 
 typedef struct { int r, g, b; } o_rgb;   /* 5:6:5 colour: r,b 0..31, g 0..63 */
 
+/* The metrics, and the functions that take one as an o_metric, are inlined
+ * into each per-metric copy of the block encoder, where the metric is a
+ * constant. */
+#define ALWAYS_INLINE __attribute__((always_inline)) inline
+
 static inline int32_t w_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 static inline int32_t w_sub(int32_t a, int32_t b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
 static inline int32_t w_mul(int32_t a, int32_t b) { return (int32_t)((uint32_t)a * (uint32_t)b); }
@@ -74,16 +79,19 @@ static o_rgb rgb_next(o_rgb c)
 /* ---------------------------------------------------------------- metrics */
 /* s2tc_algorithm.cpp:217-361.  Argument order matters: SRGB is not symmetric. */
 
+ALWAYS_INLINE
 static int32_t d_avg(o_rgb a, o_rgb b)
 {
 	int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
 	return 4 * dr * dr + dg * dg + 4 * db * db;
 }
+ALWAYS_INLINE
 static int32_t d_w0avg(o_rgb a, o_rgb b)
 {
 	int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
 	return dr * dr + dg * dg + db * db;
 }
+ALWAYS_INLINE
 static int32_t d_wavg(o_rgb a, o_rgb b)
 {
 	int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
@@ -95,16 +103,19 @@ static int32_t d_luma_chroma(int dr, int db, int y)
 	int32_t u = dr * 202 - y, v = db * 202 - y;
 	return w_add(w_add(w_mul(y, y) * 2, shrr(w_mul(u, u), 3)), shrr(w_mul(v, v), 4));
 }
+ALWAYS_INLINE
 static int32_t d_yuv(o_rgb a, o_rgb b)
 {
 	int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
 	return d_luma_chroma(dr, db, dr * 60 + dg * 59 + db * 22);
 }
+ALWAYS_INLINE
 static int32_t d_rgb(o_rgb a, o_rgb b)
 {
 	int dr = a.r - b.r, dg = a.g - b.g, db = a.b - b.b;
 	return d_luma_chroma(dr, db, dr * 42 + dg * 72 + db * 14);
 }
+ALWAYS_INLINE
 static int32_t d_srgb(o_rgb a, o_rgb b)
 {
 	int32_t dr = a.r * a.r - b.r * b.r;
@@ -126,6 +137,7 @@ static int srgb_luma(o_rgb a)
 	f = f + 0.5f;
 	return (int)f;
 }
+ALWAYS_INLINE
 static int32_t d_srgb_mixed(o_rgb a, o_rgb b)
 {
 	int ay = srgb_luma(a), by = srgb_luma(b);
@@ -151,6 +163,7 @@ static void nm_unit(o_rgb c, float v[3])
 		v[2] = v[2] * n;
 	}
 }
+ALWAYS_INLINE
 static int32_t d_normalmap(o_rgb a, o_rgb b)
 {
 	float va[3], vb[3], s, t;
@@ -166,6 +179,8 @@ static int32_t d_normalmap(o_rgb a, o_rgb b)
 }
 
 typedef int32_t (*o_metric)(o_rgb, o_rgb);
+/* random candidates held on the stack; more take a heap buffer */
+enum { kStackRandom = 64 };
 static o_metric metric_fn(int metric)
 {
 	switch (metric) {
@@ -194,6 +209,7 @@ int32_t s2tc_oracle_color_dist(int metric, int ar, int ag, int ab, int br, int b
 /* Pair search over candidates (s2tc_algorithm.cpp:363-414): inputs are the
  * first n candidates, all m are endpoint candidates.  Distances between two
  * inputs are evaluated once, as dist(c[lo], c[hi]), and used both ways. */
+ALWAYS_INLINE
 static void reduce_rgb(o_rgb *c, int n, int m, o_metric dist, int32_t *dm)
 {
 	int i, j, k;
@@ -276,6 +292,7 @@ static inline int rmean(int s, int n) { return ((s << 1) + n) / (n << 1); }
 /* Colour index pass (s2tc_algorithm.cpp:582-643 with bpp=2, two references).
  * Visits texels x-outer, y-inner.  Returns the unsigned score; when `acc` is
  * set, also returns per-endpoint sums of the texels that chose it. */
+ALWAYS_INLINE
 static uint32_t colour_pass(uint32_t *bits, const uint8_t *blk, int iw, int w, int h,
 			    o_metric dist, int have_trans, o_rgb r0, o_rgb r1,
 			    int acc, int cnt[2], int sum[2][3])
@@ -344,6 +361,7 @@ static void colour_finish(uint32_t *bits, o_rgb *c0, o_rgb *c1, int have_trans)
 }
 
 /* Colour refinement NEVER / ALWAYS / LOOP (s2tc_algorithm.cpp:767-860). */
+ALWAYS_INLINE
 static uint32_t colour_refine(const uint8_t *blk, int iw, int w, int h, o_metric dist,
 			      int have_trans, int refine, o_rgb *c0, o_rgb *c1)
 {
@@ -487,15 +505,18 @@ static void put_colour_block(uint8_t *out, o_rgb c0, o_rgb c1, uint32_t bits)
 /* Encode one 4x4 (or edge w x h) block of the 4-byte 5:6:5+alpha texel buffer
  * (s2tc_algorithm.cpp:872-1108).  `rgba` points at the block's first texel and
  * `iw` is the buffer's row length in texels. */
-int s2tc_oracle_encode_block_ex(uint8_t *out, const uint8_t *rgba, int iw, int w, int h,
-				int dxt, int metric, int nrandom, int refine, int prev_a1)
+ALWAYS_INLINE
+static int encode_block(uint8_t *out, const uint8_t *rgba, int iw, int w, int h,
+			int dxt, int metric, o_metric dist, int nrandom, int refine, int prev_a1)
 {
 	int leftover;
-	o_metric dist = metric_fn(metric);
 	int nr = nrandom > 0 ? nrandom : 0;
 	int normal_mode = metric == S2TC_O_NORMALMAP || nrandom >= 0;   /* :1139 */
-	o_rgb *c = (o_rgb *)malloc(sizeof(o_rgb) * (16 + nr));
-	uint8_t *ca = (uint8_t *)malloc(16 + nr);
+	o_rgb c_stack[16 + kStackRandom];
+	uint8_t ca_stack[16 + kStackRandom];
+	int32_t dm_stack[(16 + kStackRandom + 2) * 16];
+	o_rgb *c = nr <= kStackRandom ? c_stack : (o_rgb *)malloc(sizeof(o_rgb) * (16 + nr));
+	uint8_t *ca = nr <= kStackRandom ? ca_stack : (uint8_t *)malloc(16 + nr);
 	int x, y;
 	int a0 = 0, a1 = 0;
 
@@ -574,10 +595,11 @@ int s2tc_oracle_encode_block_ex(uint8_t *out, const uint8_t *rgba, int iw, int w
 			m = n = 2;
 		}
 		{
-			int32_t *dm = (int32_t *)malloc(sizeof(int32_t) * (size_t)(m + 2) * (size_t)n);
+			int32_t *dm = nr <= kStackRandom ? dm_stack
+				: (int32_t *)malloc(sizeof(int32_t) * (size_t)(m + 2) * (size_t)n);
 			reduce_rgb(c, n, m, dist, dm);
 			if (dxt == S2TC_O_DXT5) reduce_alpha(ca, n, m, dm);
-			free(dm);
+			if (dm != dm_stack) free(dm);
 		}
 	}
 
@@ -619,9 +641,30 @@ int s2tc_oracle_encode_block_ex(uint8_t *out, const uint8_t *rgba, int iw, int w
 			put_colour_block(out + 8, c0, c1, cbits);
 		}
 	}
-	free(c);
-	free(ca);
+	if (c != c_stack) free(c);
+	if (ca != ca_stack) free(ca);
 	return leftover;
+}
+
+/* One copy of the block encoder per distance metric, so that each copy calls
+ * its metric directly (the reference's ColorDist template parameter,
+ * s2tc_algorithm.cpp:1110-1180) and the compiler inlines it. */
+int s2tc_oracle_encode_block_ex(uint8_t *out, const uint8_t *rgba, int iw, int w, int h,
+				int dxt, int metric, int nrandom, int refine, int prev_a1)
+{
+#define ENC(D) encode_block(out, rgba, iw, w, h, dxt, metric, D, nrandom, refine, prev_a1)
+	switch (metric) {
+	case S2TC_O_RGB: return ENC(d_rgb);
+	case S2TC_O_YUV: return ENC(d_yuv);
+	case S2TC_O_SRGB: return ENC(d_srgb);
+	case S2TC_O_SRGB_MIXED: return ENC(d_srgb_mixed);
+	case S2TC_O_AVG: return ENC(d_avg);
+	case S2TC_O_W0AVG: return ENC(d_w0avg);
+	case S2TC_O_NORMALMAP: return ENC(d_normalmap);
+	case S2TC_O_WAVG:
+	default: return ENC(d_wavg);
+	}
+#undef ENC
 }
 
 void s2tc_oracle_encode_block(uint8_t *out, const uint8_t *rgba, int iw, int w, int h,
