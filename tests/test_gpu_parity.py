@@ -63,6 +63,39 @@ def test_srgb_wraparound(lib, oracle):
         assert np.array_equal(a, b), (w, h, hex(fmt), metric, nr, refine)
 
 
+def _pair_sums(oracle, metric, t565, bx, by, iw):
+    """The reference's 120 pair sums of one whole block's 16 inputs
+    (s2tc_algorithm.cpp:363-414), from the oracle's distance."""
+    px = t565.reshape(-1, 4)
+    ins = [tuple(int(v) for v in px[(by * 4 + y) * iw + bx * 4 + x][:3]) for x in range(4) for y in range(4)]
+    d = [[0 if i == k else oracle.color_dist(metric, ins[min(i, k)], ins[max(i, k)]) for k in range(16)]
+         for i in range(16)]
+    return [sum(min(d[i][k], d[j][k]) for k in range(16)) for i in range(16) for j in range(i + 1, 16)]
+
+
+def test_srgb_negative_pair_sums_whole_blocks(lib, oracle):
+    """Whole 4x4 blocks of the SRGB wrap-around colours, all-texels search:
+    pair sums go negative, where the reference keeps the last pair
+    (`bestsum < 0` takes every later pair), against blocks of non-negative
+    sums, where it keeps the first smallest."""
+    rng = np.random.default_rng(31)
+    w, h = 64, 32
+    rgb = cases.SRGB_WRAP_COLOURS[rng.integers(0, len(cases.SRGB_WRAP_COLOURS), (h, w))]
+    # every other block row: two colours only, half and half, so more sums are negative
+    two = cases.SRGB_WRAP_COLOURS[[0, 6]][rng.integers(0, 2, (h, w))]
+    rows = (np.arange(h) // 4) % 2 == 1
+    rgb[rows] = two[rows]
+    img = np.concatenate([rgb, np.full((h, w, 1), 255, np.uint8)], axis=2).reshape(-1)
+    t565 = oracle.rgb565_image(img, w, h, 4, 8, 0)
+    neg = sum(min(_pair_sums(oracle, 2, t565, bx, by, w)) < 0 for by in range(2) for bx in range(0, 16, 3))
+    assert 0 < neg < 12, neg  # both kinds of block occur
+    for fmt in (0x83F0, 0x83F1, 0x83F2, 0x83F3):
+        for refine in range(3):
+            a = gpu_compress(4, w, h, img, fmt, 0, 2, 0, refine, 5)
+            b = oracle.compress(4, w, h, img, fmt, 0, 2, 0, refine, seed=5)
+            assert np.array_equal(a, b), (hex(fmt), refine)
+
+
 @pytest.mark.parametrize("nr", [64, 300, 700])
 def test_many_random_candidates(lib, oracle, nr):
     """Random-candidate counts served by the warp kernel (shared-memory
