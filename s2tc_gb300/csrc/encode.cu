@@ -320,11 +320,12 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
   C3 c0, c1;
   int a0 = 0, a1 = 0;
   if (!NORMAL) {
-    // darkest / brightest by distance to black (:879-935)
+    // darkest / brightest by distance to black (:879-935), kept as texel
+    // words (their colour fields; the starting values are the colours
+    // 31,63,31 and 0,0,0)
     const P black = prep<kMetric>(C3{0, 0, 0});
     int32_t dmin = 0x7FFFFFFF, dmax = 0;
-    c0 = C3{31, 63, 31};
-    c1 = C3{0, 0, 0};
+    uint32_t t0 = 31u | (63u << 8) | (31u << 16), t1 = 0u;
     if (DXT == DXT5) a0 = a1 = texel_a(bt.px[0]);
 #pragma unroll
     for (int x = 0; x < 4; ++x)
@@ -334,8 +335,8 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
         uint32_t t = bt.px[y * 4 + x];
         if (DXT == DXT1 && (t >> 24) == 0) continue;
         int32_t d = pdist<kMetric>(tp[y * 4 + x], black);
-        if (d > dmax) { dmax = d; c1 = texel_c3(t); }
-        if (d < dmin) { dmin = d; c0 = texel_c3(t); }
+        if (d > dmax) { dmax = d; t1 = t; }
+        if (d < dmin) { dmin = d; t0 = t; }
         if (DXT == DXT5) {
           int a = texel_a(t);
           if (a != 255) {
@@ -344,6 +345,8 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
           }
         }
       }
+    c0 = texel_c3(t0);
+    c1 = texel_c3(t1);
   } else {
     if constexpr (FULL16) {
       int bi, bj;

@@ -187,22 +187,47 @@ struct BlockTexels {
 
 // ------------------------------------------------------ colour index pass
 
-struct ColourAcc {
-  int n0, n1;
-  int s0r, s0g, s0b, s1r, s1g, s1b;
+// Channel sums of a set of texels, two words: red and blue (texel word bits
+// 0-7 and 16-23) in one, green (bits 8-15) in the other.  Sixteen texels sum
+// to at most 16 * 63 per channel, so no field carries into the next.
+struct ColourSums {
+  uint32_t rb, g;
 };
+__device__ __forceinline__ uint32_t texel_rb(uint32_t t) { return t & 0x00FF00FFu; }
+__device__ __forceinline__ uint32_t texel_g(uint32_t t) { return t & 0x0000FF00u; }
+
+// The sums of the block's texels that take part in the colour passes (inside
+// the image; for DXT1 not transparent) and their number.
+template <bool TRANS>
+__device__ __forceinline__ ColourSums colour_totals(const BlockTexels& bt, int& n) {
+  ColourSums s{0u, 0u};
+  n = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int x = i & 3, y = i >> 2;
+    if (x >= bt.w || y >= bt.h) continue;
+    const uint32_t t = bt.px[i];
+    if (TRANS && (t >> 24) == 0) continue;
+    s.rb += texel_rb(t);
+    s.g += texel_g(t);
+    ++n;
+  }
+  return s;
+}
 
 // s2tc_algorithm.cpp:582-643 (colour, two references): nearest endpoint per
 // texel, ties to endpoint 0; DXT1 alpha-0 texels take index 3.  `tp` holds the
 // block's texels in prepared form (slot y*4+x).  The reference visits texels
 // x-outer, y-inner; the results (per-texel indices, sums) do not depend on
-// the order.
+// the order.  With ACC, `acc` gets the channel sums of the texels that chose
+// endpoint 1 (those of endpoint 0 are the totals minus these; the counts come
+// from the index word).
 template <int METRIC, bool TRANS, bool ACC>
 __device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, const typename PrepT<METRIC>::T* tp, C3 r0,
-                                                C3 r1, uint32_t& bits, ColourAcc& acc) {
+                                                C3 r1, uint32_t& bits, ColourSums& acc) {
   uint32_t score = 0;
   bits = 0;
-  if (ACC) acc = ColourAcc{0, 0, 0, 0, 0, 0, 0, 0};
+  if (ACC) acc = ColourSums{0u, 0u};
   const auto p0 = prep<METRIC>(r0), p1 = prep<METRIC>(r1);
 #pragma unroll
   for (int i = 0; i < 16; ++i) {
@@ -216,14 +241,8 @@ __device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, const typ
     int32_t d0 = pdist<METRIC>(tp[i], p0), d1 = pdist<METRIC>(tp[i], p1);
     const bool one = d1 < d0;
     if (ACC) {
-      C3 c = texel_c3(t);
-      if (one) {
-        acc.n1++;
-        acc.s1r += c.r; acc.s1g += c.g; acc.s1b += c.b;
-      } else {
-        acc.n0++;
-        acc.s0r += c.r; acc.s0g += c.g; acc.s0b += c.b;
-      }
+      acc.rb += texel_rb(t) * uint32_t(one);
+      acc.g += texel_g(t) * uint32_t(one);
     }
     bits |= uint32_t(one) << (2 * i);
     score += uint32_t(one ? d1 : d0);
@@ -231,13 +250,31 @@ __device__ __forceinline__ uint32_t colour_pass(const BlockTexels& bt, const typ
   return score;
 }
 
-__device__ __forceinline__ int rmean(int s, int n) { return ((s << 1) + n) / (n << 1); }
+// Rounded mean ((s << 1) + n) / (n << 1) (s2tc_algorithm.cpp:542-551) for the
+// sums of at most 16 texels: 1 <= n <= 16 and 0 <= s <= 16 * 255.  The integer
+// quotient q of x = 2s + n < 2^13 by d = 2n <= 32 is taken in float: x / d lies
+// in [q, q + 1 - 1/d] with 1/d >= 2^-5; the correctly rounded reciprocal, the
+// fused multiply-add and its one rounding (results below 2^12 + 1) miss x / d
+// by less than 2^-10, so after adding 2^-6 the value stays in (q, q + 1) and
+// its floor is q.  (Exhaustively equal to the integer division over that
+// domain: tests/test_arith.py.)
+__device__ __forceinline__ int rmean(int s, int n) {
+  const float r = __frcp_rn(float(n << 1));
+  return __float2int_rd(__fmaf_rn(float((s << 1) + n), r, 0.015625f));
+}
 
-// s2tc_algorithm.cpp:542-551
-__device__ __forceinline__ bool colour_means(const ColourAcc& a, C3& c0, C3& c1) {
-  if (!a.n0 && !a.n1) return false;
-  if (a.n0) c0 = C3{rmean(a.s0r, a.n0) & 31, rmean(a.s0g, a.n0) & 63, rmean(a.s0b, a.n0) & 31};
-  if (a.n1) c1 = C3{rmean(a.s1r, a.n1) & 31, rmean(a.s1g, a.n1) & 63, rmean(a.s1b, a.n1) & 31};
+// s2tc_algorithm.cpp:542-551, from the block's totals (`tot`, `n` texels),
+// endpoint 1's sums and the index word of the same pass.
+__device__ __forceinline__ bool colour_means(const ColourSums& tot, int n, const ColourSums& a1, uint32_t bits, C3& c0,
+                                             C3& c1) {
+  if (!n) return false;
+  const uint32_t lo = bits & 0x55555555u, hi = (bits >> 1) & 0x55555555u;
+  const int n1 = __popc(lo & ~hi);  // indices equal to 1
+  const int n0 = n - n1;
+  const uint32_t rb0 = tot.rb - a1.rb, g0 = tot.g - a1.g;  // no field goes below 0
+  if (n0) c0 = C3{rmean(int(rb0 & 0xFFFFu), n0) & 31, rmean(int(g0 >> 8), n0) & 63, rmean(int(rb0 >> 16), n0) & 31};
+  if (n1)
+    c1 = C3{rmean(int(a1.rb & 0xFFFFu), n1) & 31, rmean(int(a1.g >> 8), n1) & 63, rmean(int(a1.rb >> 16), n1) & 31};
   return true;
 }
 
@@ -263,14 +300,17 @@ template <int METRIC, bool TRANS, int REFINE>
 __device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, const typename PrepT<METRIC>::T* tp, C3& c0,
                                                   C3& c1) {
   uint32_t bits;
-  ColourAcc acc;
+  ColourSums acc;
   if (REFINE == RF_NEVER) {
     if (TRANS ? c3_lt(c1, c0) : c3_lt(c0, c1)) {
       C3 t = c0; c0 = c1; c1 = t;
     }
     colour_pass<METRIC, TRANS, false>(bt, tp, c0, c1, bits, acc);
     return bits;
-  } else if (REFINE == RF_LOOP) {
+  }
+  int n;
+  const ColourSums tot = colour_totals<TRANS>(bt, n);
+  if (REFINE == RF_LOOP) {
     C3 n0 = c0, n1 = c1;
     uint32_t best = 0x7FFFFFFFu;
     bits = 0;
@@ -282,11 +322,11 @@ __device__ __forceinline__ uint32_t colour_refine(const BlockTexels& bt, const t
       best = s2;
       c0 = n0;
       c1 = n1;
-      if (!colour_means(acc, n0, n1)) break;
+      if (!colour_means(tot, n, acc, b2, n0, n1)) break;
     }
   } else {
     colour_pass<METRIC, TRANS, true>(bt, tp, c0, c1, bits, acc);
-    colour_means(acc, c0, c1);
+    colour_means(tot, n, acc, bits, c0, c1);
   }
   colour_finish<TRANS>(bits, c0, c1);
   return bits;
