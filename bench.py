@@ -109,6 +109,23 @@ def algorithmic_bytes_per_texel(wl: dict) -> float:
     return wl["sc"] + (8 if wl["fmt"] in (0x83F0, 0x83F1) else 16) / 16.0
 
 
+def roofline_note(dominant: str, wl: dict) -> str:
+    """What bounds the dominant kernel of an image workload (from its ncu
+    captures), beside the HBM fraction that the line reports."""
+    tail = "; frac is of the HBM roofline for the algorithmic bytes"
+    if dominant == "dither":
+        if wl["dither"] == 2:
+            return ("the Floyd-Steinberg wavefront is latency-bound (a chain of width + 2 * height "
+                    "dependent steps)" + tail)
+        return ("the exact SIMPLE dither is integer-ALU bound (its per-segment state tables and "
+                "replay cost about 100 integer operations per texel)" + tail)
+    if wl["nrandom"] < 0:
+        return "the quick-mode encoder's per-block arithmetic is integer-ALU bound" + tail
+    if wl["nrandom"] > 0:
+        return "the random-candidate pair search is integer-ALU bound" + tail
+    return "the all-pairs search is integer-ALU bound" + tail
+
+
 def config_dict(wl_name: str, wl: dict) -> dict:
     import s2tc_gb300 as s2
     if wl["gen"] == "tool":
@@ -1047,11 +1064,7 @@ def main() -> None:
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "peak_source": peak_note, "traffic": None,
                 "stage_ms_per_launch": {"dither": dit_launch_ms, "encode": enc_launch_ms},
-                "note": ("the Floyd-Steinberg wavefront is latency-bound (a chain of width + 2 * height "
-                         "dependent steps); frac is of the HBM roofline for the algorithmic bytes")
-                if dominant == "dither" and wl["dither"] == 2 else
-                "the all-pairs search is integer-ALU bound; frac is of the HBM roofline for the "
-                "algorithmic bytes"}
+                "note": roofline_note(dominant, wl)}
     prof = ROOT / "profiles" / "traffic.json"
     if prof.exists():
         try:
