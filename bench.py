@@ -257,6 +257,49 @@ def _cpu_worker(args):
     return time.perf_counter() - t0, out, os.getpid()
 
 
+def _oracle_worker(job):
+    """The oracle's bytes for one image (runs in a spawned process); returns
+    their CRC-32.  `words`: the random candidates' words, or None."""
+    import zlib
+    sc, w, h, px, fmt, dither, metric, nrandom, refine, words = job
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    out = pyoracle.Oracle().compress(sc, w, h, px, fmt, dither, metric, nrandom, refine, rand_words=words)
+    return zlib.crc32(out.tobytes())
+
+
+def oracle_crcs(jobs: list) -> list:
+    """CRC-32 of the oracle's output for each job, one spawned process per
+    job (up to the host's cores)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(max(1, min(len(jobs), os.cpu_count() or 1))) as pool:
+        return pool.map(_oracle_worker, jobs, chunksize=1)
+
+
+def sample_levels(shapes: list, budget: int = 6_000_000, want: int = 8) -> list:
+    """Indices of a sample of images for the oracle check: the largest one,
+    a 1x1, a 2x2 and a 3xN level where present, a level whose sides are not
+    multiples of 4, then evenly spaced others, the rest of the sample within
+    `budget` texels."""
+    n = len(shapes)
+    picks = [max(range(n), key=lambda i: shapes[i][0] * shapes[i][1])]
+    for pred in (lambda w, h: w == 1 and h == 1, lambda w, h: w == 2 and h == 2,
+                 lambda w, h: w == 3 or h == 3, lambda w, h: (w % 4 or h % 4) and w * h > 64):
+        i = next((i for i in range(n) if pred(*shapes[i]) and i not in picks), None)
+        if i is not None:
+            picks.append(i)
+    tex = sum(shapes[i][0] * shapes[i][1] for i in picks[1:])
+    for i in range(0, n, max(1, n // (2 * want))):
+        if len(picks) >= want:
+            break
+        t = shapes[i][0] * shapes[i][1]
+        if i not in picks and tex + t <= budget:
+            picks.append(i)
+            tex += t
+    return sorted(picks)
+
+
 def reference_kind() -> tuple[bool, str]:
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
@@ -451,6 +494,24 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
         per_image(ref_out)
     s2.gpu_synchronize(sp)
     bit_exact = all(torch.equal(im["dst"], r) for im, r in zip(images, ref_out))
+    # the batch's bytes against the oracle, given the same words, on a sample
+    # (the largest level, edge levels; for the normal maps eight whole maps)
+    import zlib
+    shapes = [(im["width"], im["height"]) for im in images]
+    sample = sample_levels(shapes) if wl["gen"] == "mips" else list(range(min(8, len(images))))
+    jobs = []
+    for i in sample:
+        im = images[i]
+        words = s2.rand_words(im["width"], im["height"], im["format"], opt)
+        jobs.append((im["srccomps"], im["width"], im["height"], levels[i][1].reshape(-1), im["format"],
+                     wl["dither"], wl["metric"], wl["nrandom"], wl["refine"],
+                     im["rand"][:words].cpu().numpy().view(np.uint32) if words else None))
+    want_crc = oracle_crcs(jobs)
+    got_crc = [zlib.crc32(images[i]["dst"].cpu().numpy().tobytes()) for i in sample]
+    oracle_check = {"bit_exact_vs_oracle": want_crc == got_crc, "images_checked": len(sample),
+                    "sizes_checked": [list(shapes[i]) for i in sample],
+                    "texels_checked": sum(shapes[i][0] * shapes[i][1] for i in sample)}
+    del jobs
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -558,6 +619,7 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
             "per_image": {"value": single, "unit": "texels/s", "ms_per_step": 1000 * t_single / args.steps,
                           "launches_per_step": None},
             "batched_over_per_image": value / single, "bit_exact_batched_vs_per_image": bit_exact,
+            **oracle_check,
             "per_image_tx_compress_dxtn": {"value": texels / t_host, "unit": "texels/s", "ms_per_step": 1000 * t_host,
                                            "note": "one synchronous call per image, pinned host buffers"},
             "e2e_over_per_image_tx_compress_dxtn": (args.steps * texels / t_e2e) / (texels / t_host),
@@ -861,6 +923,22 @@ def run_serving_workload(args, wl_name: str, wl: dict) -> None:
         wall, lat, st, crcs = serve(None, check)
     launches = s2.kernel_launches() - l0
     bit_exact = all(crcs.get(i) == want[i] for i in check)
+    # the server's bytes against the oracle on a sample of the checked
+    # requests: the largest, the smallest, one per distance metric, others
+    # spread over the sizes
+    chk = sorted(check)
+    picked = [chk[j] for j in sample_levels([(sizes[i][0], sizes[i][1]) for i in chk], budget=20_000_000)]
+    for m in (3, 5, 7):
+        if not any(reqs[i]["metric"] == m for i in picked):
+            i = next((i for i in chk if reqs[i]["metric"] == m and texels[i] <= 1 << 20), None)
+            if i is not None:
+                picked.append(i)
+    smallest = min(chk, key=lambda i: texels[i])
+    if smallest not in picked:
+        picked.append(smallest)
+    jobs = [(4, sizes[i][0], sizes[i][1], pool_img[offs[i]:offs[i] + texels[i] * 4], sizes[i][2], wl["dither"],
+             reqs[i]["metric"], wl["nrandom"], wl["refine"], None) for i in picked]
+    oracle_ok = oracle_crcs(jobs) == [crcs.get(i) for i in picked]
     value = total_tex / wall
     rate_max = nreq / wall
     poisson = []
@@ -892,6 +970,8 @@ def run_serving_workload(args, wl_name: str, wl: dict) -> None:
                             "ms_per_request_mean": 1000 * t_single / nreq},
             "server_over_per_request": value / (total_tex / t_single),
             "poisson": poisson, "bit_exact_sampled": bit_exact, "bit_exact_requests_checked": len(check),
+            "bit_exact_vs_oracle": oracle_ok, "oracle_requests_checked": len(picked),
+            "oracle_sizes_checked": [[sizes[i][0], sizes[i][1]] for i in sorted(picked)],
             "gpu_launches": launches, "cpu_baseline": None, "clocks": clk.summary(),
             "roofline": None}
     print(json.dumps(line), flush=True)

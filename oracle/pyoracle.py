@@ -84,17 +84,33 @@ class Oracle:
         lib.s2tc_oracle_from_s3tc_block.argtypes = [i, vp]
         lib.s2tc_oracle_from_s3tc.argtypes = [vp, lg, vp]
         lib.s2tc_oracle_from_s3tc.restype = lg
+        lib.s2tc_oracle_set_rand_words.argtypes = [vp, lg]
+        lib.s2tc_oracle_rand_words_used.restype = lg
         self.lib = lib
 
     def compress(self, srccomps, w, h, src, fmt, dither, metric, nrandom, refine,
-                 dst_row_stride=0, dest=None, seed=None) -> np.ndarray:
+                 dst_row_stride=0, dest=None, seed=None, rand_words=None) -> np.ndarray:
+        """tx_compress_dxtn with explicit knobs.  `rand_words`: the random
+        candidates' words in the reference's call order, instead of libc's
+        rand() (the call must take exactly that many, or ValueError)."""
         src = np.ascontiguousarray(src, dtype=np.uint8)
         if dest is None:
             dest = np.zeros(out_size(w, h, fmt), np.uint8)
         if seed is not None:
             srand(seed)
-        self.lib.s2tc_oracle_compress(srccomps, w, h, _vp(src), fmt, _vp(dest), dst_row_stride,
-                                      dither, metric, nrandom, refine)
+        words = None
+        if rand_words is not None:
+            words = np.ascontiguousarray(rand_words, dtype=np.uint32)
+            self.lib.s2tc_oracle_set_rand_words(_vp(words), words.size)
+        try:
+            self.lib.s2tc_oracle_compress(srccomps, w, h, _vp(src), fmt, _vp(dest), dst_row_stride,
+                                          dither, metric, nrandom, refine)
+            used = self.lib.s2tc_oracle_rand_words_used() if words is not None else 0
+        finally:
+            if words is not None:
+                self.lib.s2tc_oracle_set_rand_words(None, 0)
+        if words is not None and used != words.size:
+            raise ValueError(f"the call took {used} random words, {words.size} were given")
         return dest
 
     def rgb565_image(self, src, w, h, srccomps, alphabits, dither) -> np.ndarray:

@@ -21,7 +21,8 @@
  *   - float code is IEEE single precision, every operation rounded, no fused
  *     multiply-add (x86-64 SSE without -march).  Build with -ffp-contract=off
  *     so that aarch64 gcc does not fuse.
- *   - rand() is libc's, called in the same order as the reference.
+ *   - rand() is libc's, called in the same order as the reference (or, for
+ *     tests, the same words from an array: s2tc_oracle_set_rand_words).
  */
 #include <stdint.h>
 #include <stdlib.h>
@@ -492,6 +493,31 @@ static uint64_t alpha_refine(const uint8_t *blk, int iw, int w, int h, int refin
 
 /* ------------------------------------------------------------ block encoder */
 
+/* Where the random candidates' words come from: libc's rand(), as in the
+ * reference (s2tc_algorithm.cpp:986-990), or a caller-supplied array of the
+ * same words (s2tc_oracle_set_rand_words), which lets a test hold an encoder
+ * fed with stored words against this restatement without replaying libc's
+ * stream.  Words are consumed in the reference's call order either way. */
+static const uint32_t *o_words;
+static long o_words_n, o_words_pos;
+
+void s2tc_oracle_set_rand_words(const uint32_t *words, long n)
+{
+	o_words = words;
+	o_words_n = words ? n : 0;
+	o_words_pos = 0;
+}
+
+long s2tc_oracle_rand_words_used(void) { return o_words_pos; }
+
+static inline int o_rand(void)
+{
+	if (!o_words) return rand();
+	/* past the end: a value that no test expects, and the count tells */
+	if (o_words_pos >= o_words_n) { ++o_words_pos; return 0; }
+	return (int)o_words[o_words_pos++];
+}
+
 static void put_colour_block(uint8_t *out, o_rgb c0, o_rgb c1, uint32_t bits)
 {
 	out[0] = (uint8_t)(((c0.g & 7) << 5) | c0.b);
@@ -577,10 +603,10 @@ static int encode_block(uint8_t *out, const uint8_t *rgba, int iw, int w, int h,
 			lr = hi.r - lo.r + 1; lg = hi.g - lo.g + 1; lb = hi.b - lo.b + 1;
 			la = ahi - alo + 1;
 			for (r = 0; r < nrandom; ++r) {
-				c[m].r = lo.r + rand() % lr;
-				c[m].g = lo.g + rand() % lg;
-				c[m].b = lo.b + rand() % lb;
-				if (dxt == S2TC_O_DXT5) ca[m] = (uint8_t)(alo + rand() % la);
+				c[m].r = lo.r + o_rand() % lr;
+				c[m].g = lo.g + o_rand() % lg;
+				c[m].b = lo.b + o_rand() % lb;
+				if (dxt == S2TC_O_DXT5) ca[m] = (uint8_t)(alo + o_rand() % la);
 				++m;
 			}
 		} else if (n == 1) {

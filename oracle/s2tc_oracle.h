@@ -28,6 +28,10 @@ int s2tc_oracle_encode_block_ex(uint8_t *out, const uint8_t *rgba, int iw, int w
 void s2tc_oracle_rgb565_image(uint8_t *out, const uint8_t *src, int w, int h, int srccomps,
 			      int alphabits, int dither);
 int s2tc_oracle_format_dxt(unsigned int fmt);
+/* The random candidates read their words from `words` (n of them) instead of
+ * libc's rand(); NULL restores rand().  _used() counts the words taken since. */
+void s2tc_oracle_set_rand_words(const uint32_t *words, long n);
+long s2tc_oracle_rand_words_used(void);
 int s2tc_oracle_compress(int srccomps, int width, int height, const uint8_t *src,
 			 unsigned int fmt, uint8_t *dest, int dst_row_stride,
 			 int dither, int metric, int nrandom, int refine);

@@ -275,12 +275,57 @@ def test_value_noise_4096_exhaustive(lib, oracle):
 
 
 def test_normal_map_random_candidates(lib, oracle):
-    """One 2048x2048 RGB normal map -> DXT1, NORMALMAP, 64 random candidates,
-    LOOP (rand() replayed in block order), compared on a 512-row band."""
+    """A 512x512 RGB normal map -> DXT1, NORMALMAP, 64 random candidates, LOOP
+    (rand() replayed in block order)."""
     img = workloads.normal_map(4, 512, 512).reshape(-1)
     a = gpu_compress(3, 512, 512, img, 0x83F1, 1, 7, 64, 2, seed=1234)
     b = oracle.compress(3, 512, 512, img, 0x83F1, 1, 7, 64, 2, seed=1234)
     assert np.array_equal(a, b)
+
+
+def test_normal_map_full_2048(lib, oracle):
+    """One whole 2048x2048 normal map of the 64-map workload's recipe -> DXT1,
+    NORMALMAP, 64 random candidates, LOOP, SIMPLE dither: every block against
+    the oracle, with libc's rand() stream consumed over the whole image
+    (50 M words, generated on the GPU from the stream's position)."""
+    img = workloads.normal_map(4, 2048, 2048).reshape(-1)
+    a = gpu_compress(3, 2048, 2048, img, 0x83F1, 1, 7, 64, 2, seed=4321)
+    after_gpu = pyoracle.libc_rand()
+    b = oracle.compress(3, 2048, 2048, img, 0x83F1, 1, 7, 64, 2, seed=4321)
+    assert np.array_equal(a, b)
+    assert pyoracle.libc_rand() == after_gpu  # both left the stream at the same place
+
+
+def test_batch_resident_rand_words_vs_oracle(lib, oracle):
+    """The batched graph launch fed caller-resident random-candidate words
+    (the form the batched benchmarks time): uneven mip chains with 1x1, 2x2
+    and 3xN levels, mixed formats and component counts, against the oracle
+    given the same words."""
+    torch = pytest.importorskip("torch")
+    tex = workloads.mip_textures(41, count=8, lo=3, hi=90)
+    opt = s2.options(1, s2.WAVG, 16, 1)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    images, host = [], []
+    for t in tex:
+        for lvl in t["levels"]:
+            h, w = lvl.shape[:2]
+            words = s2.rand_words(w, h, t["fmt"], opt)
+            rw = torch.randint(0, 2**31 - 1, (max(1, words),), dtype=torch.int32, device="cuda", generator=gen)
+            n = s2.compressed_size(w, h, t["fmt"])
+            images.append({"src": torch.from_numpy(lvl.reshape(-1).copy()).cuda(), "width": w, "height": h,
+                           "srccomps": t["srccomps"], "format": t["fmt"], "rand": rw,
+                           "dst": torch.full((n,), 0xA5, dtype=torch.uint8, device="cuda")})
+            host.append((t["srccomps"], t["fmt"], lvl.reshape(-1), words))
+    b = s2.Batch(images, opt)
+    b.run()
+    s2.gpu_synchronize()
+    b.close()
+    for im, (sc, fmt, px, words) in zip(images, host):
+        w, h = im["width"], im["height"]
+        want = oracle.compress(sc, w, h, px, fmt, 1, s2.WAVG, 16, 1,
+                               rand_words=im["rand"].cpu().numpy().view(np.uint32)[:words])
+        assert np.array_equal(im["dst"].cpu().numpy(), want), (w, h, hex(fmt), sc)
 
 
 def test_tool_call_sequence(lib, oracle):
