@@ -179,6 +179,17 @@ void s2tc_server_destroy(s2tc_server *server);
  * kernel since the last check gave up a bounded wait (S2TC_ERR_TIMEOUT). */
 int s2tc_gpu_synchronize(void *stream);
 
+/* Test hook of the timeout path; no counterpart in the reference.  Launches
+ * of the SIMPLE dither made (or captured into a graph) after this call keep
+ * dither tile `hold_tile` of their work list (16640 texels per tile, raster
+ * order; -1: none) from publishing its scan state, and give up each
+ * look-back wait after `spin_limit` polls (0: the library's default limit,
+ * about 4 M polls).  The tiles that wait on the held tile give up, and the
+ * call reports S2TC_ERR_TIMEOUT (s2tc_gpu_synchronize, or the error text of
+ * tx_compress_dxtn) with undefined output; nothing faults or hangs.  Call it
+ * with (-1, 0) to restore normal operation. */
+int s2tc_test_dither_hold(long long hold_tile, int spin_limit);
+
 /* Number of rand() words an image consumes: blocks * nrandom * (4 for DXT5,
  * else 3) when the random-candidate search is active, else 0. */
 long long s2tc_rand_words(int width, int height, unsigned int destformat, const s2tc_options *opt);
@@ -212,7 +223,10 @@ int s2tc_gpu_encode_blocks(const void *d_t565, int width, int height, int dxt, i
  * calls).  Same arguments and bytes as s2tc_gpu_compress, but the scratch
  * (dither state and 5:6:5 texel words) lives in one fixed device array of the
  * library, held on every GPU that loads it until exit; images are limited to
- * 4 Mi texels (S2TC_ERR_TOO_LARGE beyond), RANDOM_COLORS > 0 needs `d_rand`,
+ * 4 Mi texels (S2TC_ERR_TOO_LARGE beyond; with Floyd-Steinberg dither also
+ * ceil(width/8)*8 * ceil(height/256) <= 65520, so that its carry rows fit the
+ * array's 1 MiB scan region: a 65536x64 image is rejected, every image up to
+ * 2048x2048 fits), RANDOM_COLORS > 0 needs `d_rand`,
  * and the call waits for `stream` before returning.  The first call on a
  * device sets up the array's address: make it before any stream capture.
  * Calls are serialised within the process; calls whose GPU work overlaps

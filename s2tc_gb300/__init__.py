@@ -114,6 +114,8 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     lib.s2tc_gpu_stage_ms.restype = c_int
     lib.s2tc_gpu_kernel_launches.argtypes = []
     lib.s2tc_gpu_kernel_launches.restype = c_ll
+    lib.s2tc_test_dither_hold.argtypes = [c_ll, c_int]
+    lib.s2tc_test_dither_hold.restype = c_int
     lib.s2tc_gpu_compress_each.argtypes = [ctypes.POINTER(Image), c_int, ctypes.POINTER(Options), vp]
     lib.s2tc_gpu_compress_each.restype = c_int
     lib.s2tc_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Image), c_int,
@@ -175,7 +177,7 @@ EXPORTED_SYMBOLS = (
     "fetch_2d_texel_rgba_dxt3", "fetch_2d_texel_rgba_dxt5", "rgb565_image",
     "s2tc_encode_block_func", "s2tc_options_from_env", "s2tc_gpu_compress",
     "s2tc_gpu_synchronize", "s2tc_rand_words", "s2tc_gpu_set_timing", "s2tc_gpu_stage_ms",
-    "s2tc_gpu_kernel_launches", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
+    "s2tc_gpu_kernel_launches", "s2tc_test_dither_hold", "s2tc_gpu_compress_noalloc", "s2tc_batch_create", "s2tc_batch_run", "s2tc_gpu_compress_each",
     "s2tc_batch_kernels", "s2tc_batch_destroy", "s2tc_server_create", "s2tc_server_submit", "s2tc_server_submit_device",
     "s2tc_server_wait", "s2tc_server_stats", "s2tc_server_destroy",
     "s2tc_gpu_encode_blocks", "s2tc_autotune", "s2tc_encode_layout_set", "s2tc_encode_layout_get", "s2tc_dds_size", "s2tc_compress_dds", "s2tc_gpu_decode", "s2tc_decompress_dds",
@@ -305,6 +307,12 @@ def stage_ms() -> tuple[float, float, int]:
     if st != S2TC_OK:
         raise S2tcError(f"s2tc_gpu_stage_ms failed ({st}): {last_error()}")
     return a.value, b.value, n.value
+
+
+def hold_dither_tile(hold_tile: int = -1, spin_limit: int = 0) -> None:
+    """The timeout-path test hook (s2tc_test_dither_hold); (-1, 0) restores
+    normal operation."""
+    load().s2tc_test_dither_hold(int(hold_tile), int(spin_limit))
 
 
 def kernel_launches() -> int:

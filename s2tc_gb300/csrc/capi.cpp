@@ -1139,6 +1139,11 @@ int s2tc_gpu_stage_ms(float* dither_ms, float* encode_ms, long long* calls) {
 
 long long s2tc_gpu_kernel_launches(void) { return s2tc::launches_so_far(); }
 
+int s2tc_test_dither_hold(long long hold_tile, int spin_limit) {
+  s2tc::set_dither_test_hold(hold_tile, spin_limit);
+  return S2TC_OK;
+}
+
 int s2tc_gpu_compress_each(const s2tc_image* items, int count, const s2tc_options* opt, void* stream) {
   if (!opt || count < 0 || (count > 0 && !items)) {
     set_error("bad argument");

@@ -442,12 +442,14 @@ template <int AK>
 __device__ uint32_t look_back(const DitherWork& w, long long g, long long lt, const Rec& agg, TileSmem& sm) {
   const int lane = threadIdx.x & 31;
   Status st(w.status[g]);
+  const bool publish = g != w.hold_tile;  // false only under the test hook
+  const int spin_limit = w.spin_limit > 0 ? w.spin_limit : kSpinLimit;
   if (lt == 0) {
     const uint32_t carry = initial_state<AK>();
-    if (lane == 0) st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+    if (lane == 0 && publish) st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
     return carry;
   }
-  if (lane == 0) {
+  if (lane == 0 && publish) {
     rec_store(reinterpret_cast<uint32_t*>(w.aggs + g * kRec), agg);
     st.store(kAggReady, cuda::memory_order_release);
   }
@@ -463,7 +465,7 @@ __device__ uint32_t look_back(const DitherWork& w, long long g, long long lt, co
       Status sk(w.status[k]);
       v = sk.load(cuda::memory_order_acquire);
       int spins = 0;
-      while ((v >> 32) == 0 && spins < kSpinLimit) {
+      while ((v >> 32) == 0 && spins < spin_limit) {
         __nanosleep(64);
         v = sk.load(cuda::memory_order_acquire);
         ++spins;
@@ -494,7 +496,7 @@ __device__ uint32_t look_back(const DitherWork& w, long long g, long long lt, co
     }
     __syncwarp();
   }
-  if (lane == 0) st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
+  if (lane == 0 && publish) st.store(kIncReady | apply<AK>(agg, carry), cuda::memory_order_release);
   return carry;
 }
 
@@ -667,8 +669,13 @@ __global__ void __launch_bounds__(kThreads, S2TC_DITHER_MINBLOCKS) k_dither_simp
   const uint8_t* tsrc = it.src + p0 * 4;
   if (it.srccomps == 4 && n == kTile && (reinterpret_cast<uintptr_t>(tsrc) & 15) == 0) {
     if (!bulk_load(sm, tsrc, uint32_t(kTile) * 4u)) {
+      // The copy did not complete within the bounded wait.  The error flag
+      // makes the whole call report S2TC_ERR_TIMEOUT, and its output is then
+      // undefined; the tile still runs to the end (with the texels loaded
+      // again by plain loads after a second bounded wait for the copy) so
+      // that it publishes its scan state and the tiles behind it do not all
+      // wait out their own limits.
       atomicExch(w.error, 1);
-      // give the copy another bounded wait before the buffer is reused
       bulk_load_wait(sm);
       load_tile(it, p0, n, sm.px);
     }
@@ -711,6 +718,8 @@ __global__ void __launch_bounds__(kThreads) k_dither_none(DitherWork w) {
 }
 
 std::atomic<long long> g_launches{0};
+std::atomic<long long> g_hold_tile{-1};
+std::atomic<int> g_spin_limit{0};
 
 cudaError_t set_smem(const void* fn, size_t bytes) {
   return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
@@ -719,6 +728,11 @@ cudaError_t set_smem(const void* fn, size_t bytes) {
 }  // namespace
 
 void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+void set_dither_test_hold(long long hold_tile, int spin_limit) {
+  g_hold_tile.store(hold_tile < 0 ? -1 : hold_tile);
+  g_spin_limit.store(spin_limit > 0 ? spin_limit : 0);
+}
 long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 long long dither_tile_texels() { return kTile; }
@@ -749,6 +763,8 @@ cudaError_t launch_tiles(DitherWork w, int dither, uint8_t* scratch, long long a
     k_dither_none<<<unsigned(w.total_tiles), kThreads, kTile * sizeof(uint32_t), s>>>(w);
     return cudaGetLastError();
   }
+  w.hold_tile = g_hold_tile.load();
+  w.spin_limit = g_spin_limit.load();
   w.status = reinterpret_cast<unsigned long long*>(scratch);
   w.aggs = scratch + all_tiles * sizeof(unsigned long long);
   uintptr_t tk = reinterpret_cast<uintptr_t>(w.aggs + all_tiles * kRec);

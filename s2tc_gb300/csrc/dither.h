@@ -46,7 +46,18 @@ struct DitherWork {
   unsigned long long* status;   // total_tiles status words (zeroed before launch)
   uint8_t* aggs;                // total_tiles aggregate tables
   unsigned int* ticket;         // zeroed before launch
+  // test hook (set_dither_test_hold): the look-back's spin limit (0: the
+  // default) and a tile that publishes nothing (-1: none)
+  int spin_limit;
+  long long hold_tile;
 };
+
+// Test hook of the timeout path: launches of the SIMPLE dither made after this
+// call keep tile `hold_tile` (global index within a launch's work list; -1:
+// none) from publishing its scan state, and give up each look-back wait after
+// `spin_limit` polls (0: the default limit).  The tiles behind a held tile
+// time out, set the error flag and finish; the call reports S2TC_ERR_TIMEOUT.
+void set_dither_test_hold(long long hold_tile, int spin_limit);
 
 // Texels per tile of the batched/SIMPLE dither kernels.
 long long dither_tile_texels();
