@@ -90,14 +90,28 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
     return LIB_PATH
 
 
+# Where this recipe looks for the reference's sources (the build container's
+# read-only checkout); S2TC_REFERENCE_DIR overrides it.  Machines without the
+# sources (the GPU hosts) build only the restatement.
+DEFAULT_REFERENCE_DIR = "/root/reference"
+
+
+def reference_dir() -> Path | None:
+    """The reference's source tree, or None where it is absent."""
+    ref = Path(os.environ.get("S2TC_REFERENCE_DIR", DEFAULT_REFERENCE_DIR))
+    return ref if (ref / "s2tc_algorithm.cpp").exists() else None
+
+
 def build_oracle(verbose: bool = False) -> None:
     """The CPU restatement (always) and the reference's own encoder (only where
     its sources are present)."""
     oracle = ROOT / "oracle"
     targets = ["oracle"]
-    ref = Path(os.environ.get("S2TC_REFERENCE_DIR", "/root/reference"))
-    if (ref / "s2tc_algorithm.cpp").exists():
+    ref = reference_dir()
+    if ref is not None:
         targets.append("ref")
+    else:
+        ref = Path(DEFAULT_REFERENCE_DIR)
     r = subprocess.run(["make", "-C", str(oracle), f"REF={ref}", *targets], capture_output=True, text=True)
     if verbose or r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

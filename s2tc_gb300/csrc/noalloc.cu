@@ -17,6 +17,11 @@
 // Limits and rules:
 //   - images of at most kNoallocMaxTexels texels (4 Mi, e.g. 2048x2048); larger
 //     ones are rejected with S2TC_ERR_TOO_LARGE;
+//   - with Floyd-Steinberg dither the wavefront's carry rows (16 bytes per
+//     texel column, rounded up to 8 columns, per 256 texel rows) must also fit
+//     the kScanBytes region: width rounded up to 8 times ceil(height / 256) at
+//     most 65520, so a 65536x64 image is rejected although it is under 4 Mi
+//     texels;
 //   - RANDOM_COLORS > 0 needs the caller's replayed rand() words (d_rand); the
 //     host replay path would need a device buffer;
 //   - the first call on a device resolves the array's device address

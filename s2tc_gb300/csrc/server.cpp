@@ -178,20 +178,8 @@ int launch_round(s2tc_server* sv, Slot& sl) {
   std::vector<std::shared_ptr<Req>>& rs = sl.reqs;
   cudaStream_t s = sl.compute;
   unsigned char* base = sv->base;
-  if (cudaMemsetAsync(sl.d_err, 0, sizeof(int), s) != cudaSuccess) return S2TC_ERR_CUDA;
-  // uploads
-  for (auto& r : rs) {
-    if (!r->device_io &&
-        cudaMemcpyAsync(base + r->off, r->hsrc, r->in_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
-      return S2TC_ERR_CUDA;
-    if (r->rand_bytes && !r->dev_rand &&
-        cudaMemcpyAsync(base + r->off + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign) +
-                            align_up(r->out_bytes, kAlign),
-                        r->rand.data(), r->rand_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
-      return S2TC_ERR_CUDA;
-  }
-  if (cudaEventRecord(sl.uploaded, sv->copy_in) != cudaSuccess) return S2TC_ERR_CUDA;
-  if (cudaStreamWaitEvent(s, sl.uploaded, 0) != cudaSuccess) return S2TC_ERR_CUDA;
+  // The round's tables are laid out first, and their size checked, before any
+  // copy that reads a client's host buffer is enqueued.
 
   // group requests by knobs (the kernels take uniform knobs per launch)
   std::map<std::tuple<int, int, int, int>, std::vector<Req*>> groups;
@@ -302,6 +290,20 @@ int launch_round(s2tc_server* sv, Slot& sl) {
   for (auto& r : rs)
     if (r->dev_rand) gens.emplace_back(put(&r->win, sizeof(RandWindow)), r.get());
   if (toff > sl.tab_bytes || soff > sl.scratch_bytes) return S2TC_ERR_TOO_LARGE;
+  if (cudaMemsetAsync(sl.d_err, 0, sizeof(int), s) != cudaSuccess) return S2TC_ERR_CUDA;
+  // uploads
+  for (auto& r : rs) {
+    if (!r->device_io &&
+        cudaMemcpyAsync(base + r->off, r->hsrc, r->in_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
+      return S2TC_ERR_CUDA;
+    if (r->rand_bytes && !r->dev_rand &&
+        cudaMemcpyAsync(base + r->off + align_up(r->in_bytes, kAlign) + align_up(r->tex_bytes, kAlign) +
+                            align_up(r->out_bytes, kAlign),
+                        r->rand.data(), r->rand_bytes, cudaMemcpyHostToDevice, sv->copy_in) != cudaSuccess)
+      return S2TC_ERR_CUDA;
+  }
+  if (cudaEventRecord(sl.uploaded, sv->copy_in) != cudaSuccess) return S2TC_ERR_CUDA;
+  if (cudaStreamWaitEvent(s, sl.uploaded, 0) != cudaSuccess) return S2TC_ERR_CUDA;
   if (toff && cudaMemcpyAsync(sl.dtab, sl.htab, toff, cudaMemcpyHostToDevice, s) != cudaSuccess) return S2TC_ERR_CUDA;
   for (auto& g : gens) {
     Req* r = g.second;
@@ -391,6 +393,15 @@ void scheduler(s2tc_server* sv) {
         // need not wait while its stream operations are issued
         lk.unlock();
         const int st = launch_round(sv, *free_slot);
+        if (st != S2TC_OK) {
+          // copies of this round may already be in flight (they read the
+          // clients' host buffers and write the pool or the clients' outputs):
+          // let them finish before the memory is released and the requests
+          // are reported done
+          cudaStreamSynchronize(sv->copy_in);
+          cudaStreamSynchronize(free_slot->compute);
+          cudaStreamSynchronize(sv->copy_out);
+        }
         lk.lock();
         if (st != S2TC_OK) {
           for (auto& r : free_slot->reqs) {

@@ -169,8 +169,9 @@ def _load_tga(path: Path) -> np.ndarray:
 def test_reference_fixture_images(oracle, reference):
     """The reference's own test images (tests/*.tga), cropped, in the three
     configurations its visual test script runs."""
-    tdir = Path("/root/reference/tests")
-    files = sorted(tdir.glob("*.tga")) if tdir.exists() else []
+    from s2tc_gb300 import build
+    ref = build.reference_dir()
+    files = sorted((ref / "tests").glob("*.tga")) if ref is not None else []
     if not files:
         pytest.skip("reference test images not present")
     for f in files:

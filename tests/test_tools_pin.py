@@ -60,8 +60,9 @@ def test_compress_tool_synthetic(oracle, tools, fmt):
 def test_compress_tool_fixture_images(oracle, tools):
     """The reference's own test images through s2tc_compress in the
     configurations its test script uses."""
-    tdir = Path("/root/reference/tests")
-    files = sorted(tdir.glob("*.tga")) if tdir.exists() else []
+    from s2tc_gb300 import build
+    ref = build.reference_dir()
+    files = sorted((ref / "tests").glob("*.tga")) if ref is not None else []
     if not files:
         pytest.skip("reference test images not present")
     for f in files:
