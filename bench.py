@@ -112,7 +112,7 @@ def algorithmic_bytes_per_texel(wl: dict) -> float:
 def roofline_note(dominant: str, wl: dict) -> str:
     """What bounds the dominant kernel of an image workload (from its ncu
     captures), beside the HBM fraction that the line reports."""
-    tail = "; frac is of the HBM roofline for the algorithmic bytes"
+    tail = ""
     if dominant == "dither":
         if wl["dither"] == 2:
             return ("the Floyd-Steinberg wavefront is latency-bound (a chain of width + 2 * height "
@@ -124,6 +124,42 @@ def roofline_note(dominant: str, wl: dict) -> str:
     if wl["nrandom"] > 0:
         return "the random-candidate pair search is integer-ALU bound" + tail
     return "the all-pairs search is integer-ALU bound" + tail
+
+
+def issue_roofline(wl_name: str, stage: str, stage_ms: float, texels: int, sm_mhz: float, sms: int) -> dict | None:
+    """The integer-issue roofline of one stage of a workload: warp
+    instructions that the stage's kernels issue per texel (from one ncu
+    capture of the same workload, profiles/inst_counts.json) times the texels
+    of a launch, over the stage's live CUDA-event time, against one warp
+    instruction per scheduler per cycle (4 per SM) at the sampled SM clock;
+    and the integer-ALU pipe's share against its own peak rate."""
+    # batches of the same recipe use the per-texel counts of the captured one
+    alias = {"mip_chains_256_wavg_rand64_always": "mip_chains_64_wavg_rand64_always",
+             "normal_maps_64x2048_dxt1_normalmap_rand64_loop": "normal_map_2048_dxt1_normalmap_rand64_loop"}
+    src = alias.get(wl_name, wl_name)
+    try:
+        counts = json.loads((ROOT / "profiles" / "inst_counts.json").read_text())[src]
+        if stage == "batch" and "batch" not in counts:
+            # a batch of whole images: the per-texel sum of the dither and encoder stages
+            d = {k: counts["dither"][k] + counts["encode"][k]
+                 for k in ("warp_inst_per_texel", "alu_inst_per_texel")}
+            d["alu_peak_per_sm_cycle"] = counts["encode"]["alu_peak_per_sm_cycle"]
+        else:
+            d = counts[stage]
+    except Exception:
+        return None
+    t = stage_ms / 1000.0
+    hz = sm_mhz * 1e6
+    inst = d["warp_inst_per_texel"] * texels
+    alu = d["alu_inst_per_texel"] * texels
+    issue_peak = sms * 4 * hz
+    alu_peak = sms * d["alu_peak_per_sm_cycle"] * hz
+    return {"bound": "alu", "kernel": stage, "achieved": inst / t / 1e9, "peak": issue_peak / 1e9,
+            "unit": "G warp-instructions/s", "frac": inst / t / issue_peak,
+            "alu_pipe_frac": alu / t / alu_peak, "warp_inst_per_launch": inst,
+            "peak_source": f"{sms} SMs x 4 schedulers x 1 instruction/cycle at the sampled {sm_mhz:.0f} MHz",
+            "counts_source": f"profiles/inst_counts.json, {src} (ncu smsp__inst_executed.sum, "
+                             "sm__inst_executed_pipe_alu.sum per texel)"}
 
 
 def config_dict(wl_name: str, wl: dict) -> dict:
@@ -611,6 +647,13 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     hbm = peaks.get("hbm_gbs") or 6800.0
     alg = in_bytes + out_bytes
     achieved = alg / (t_batch / args.steps) / 1e9
+    clocks = clk.summary()
+    hbm_line = {"bound": "hbm", "kernel": "batch step", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None}
+    alu = issue_roofline(wl_name, "batch", 1000 * t_batch / args.steps, texels, clocks.get("sm_mhz") or 2070.0,
+                         torch.cuda.get_device_properties(0).multi_processor_count)
+    roofline = dict(alu, hbm=hbm_line) if alu else hbm_line
+    roofline["note"] = "the random-candidate pair search (one warp per block) is integer-ALU bound"
     line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * t_batch / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
@@ -628,10 +671,8 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
                     "rand": "libc rand() stream, generated on the device",
                     "ms_per_step": 1000 * t_e2e / args.steps},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": "batch step", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
-                         "note": "random-candidate search is integer-ALU bound; frac is of the HBM roofline"},
-            "cpu_baseline": cpu, "clocks": clk.summary()}
+            "roofline": roofline,
+            "cpu_baseline": cpu, "clocks": clocks}
     print(json.dumps(line), flush=True)
 
 
@@ -1141,16 +1182,25 @@ def main() -> None:
     dominant = "encode" if enc_launch_ms >= dit_launch_ms else "dither"
     dom_ms = max(enc_launch_ms, dit_launch_ms)
     achieved = alg_bytes / (dom_ms / 1000.0) / 1e9
-    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "peak_source": peak_note, "traffic": None,
-                "stage_ms_per_launch": {"dither": dit_launch_ms, "encode": enc_launch_ms},
-                "note": roofline_note(dominant, wl)}
+    hbm = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+           "frac": achieved / hbm_peak, "peak_source": peak_note, "traffic": None}
     prof = ROOT / "profiles" / "traffic.json"
     if prof.exists():
         try:
-            roofline["traffic"] = json.loads(prof.read_text()).get(args.workload, {}).get(dominant)
+            hbm["traffic"] = json.loads(prof.read_text()).get(args.workload, {}).get(dominant)
         except Exception:
             pass
+    clocks = clk.summary()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    alu = issue_roofline(args.workload, dominant, dom_ms, npx, clocks.get("sm_mhz") or 2070.0, sms)
+    search = wl["nrandom"] >= 0 or wl["metric"] == 7
+    if alu is not None and (search or dominant == "dither"):
+        # integer-bound kernels: the issue roofline first, HBM beside it
+        roofline = dict(alu, hbm=hbm)
+    else:
+        roofline = dict(hbm, alu=alu)
+    roofline["stage_ms_per_launch"] = {"dither": dit_launch_ms, "encode": enc_launch_ms}
+    roofline["note"] = roofline_note(dominant, wl)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -1162,7 +1212,7 @@ def main() -> None:
                 "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
                 "config": dict(config_dict(args.workload, wl), launch_layout=layout or "default"),
                 "e2e": e2e, "gpu_launches": launches,
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -89,6 +89,36 @@ __device__ __forceinline__ void pick_pair(const int32_t* S, uint32_t mask, int& 
     }
 }
 
+// pick_pair (above) without negative sums and with every input taking part:
+// the smallest sum by a tree of minima, then the first pair that has it.  The
+// sequential rule is a chain of 120 dependent compare-and-selects per block;
+// this form has a dependency depth of about twenty.
+__device__ __forceinline__ void pick_pair_nonneg(const int32_t* S, int& besti, int& bestj) {
+  uint32_t t[60];
+#pragma unroll
+  for (int r = 0; r < 60; ++r) t[r] = min(uint32_t(S[2 * r]), uint32_t(S[2 * r + 1]));
+#pragma unroll
+  for (int st = 1; st < 60; st <<= 1)
+#pragma unroll
+    for (int r = 0; r + st < 60; r += 2 * st) t[r] = min(t[r], t[r + st]);
+  const uint32_t m = t[0];
+  // the first position with the minimum, as (i << 4) | j: eight independent
+  // chains of fifteen selects, then the earliest chain that found one
+  uint32_t f[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) f[c] = 0xFFu;
+  int p = 119;
+#pragma unroll
+  for (int i = 15; i >= 0; --i)
+#pragma unroll
+    for (int j = 15; j > i; --j, --p) f[p / 15] = uint32_t(S[p]) == m ? uint32_t((i << 4) | j) : f[p / 15];
+  uint32_t r = f[7];
+#pragma unroll
+  for (int c = 6; c >= 0; --c) r = f[c] != 0xFFu ? f[c] : r;
+  besti = int(r >> 4);
+  bestj = int(r & 15);
+}
+
 // reduce_colors_inplace (s2tc_algorithm.cpp:363-414) for n = m = 16.  Between
 // two inputs the reference evaluates dist(c[lo], c[hi]) once and uses it both
 // ways; d(k, k) = 0.
@@ -117,7 +147,14 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, uint32_t mask, Scratch
 #pragma unroll
       for (int j = i + 1; j < 16; ++j, ++p) S[p] = wadd(S[p], min(col[i], col[j]));
   }
-  pick_pair(S, mask, besti, bestj);
+  uint32_t neg = 0;
+#pragma unroll
+  for (int p = 0; p < 120; ++p) neg |= uint32_t(S[p]);
+  if (mask == 0xFFFFu && int32_t(neg) >= 0) {
+    pick_pair_nonneg(S, besti, bestj);
+    return;
+  }
+  pick_pair(S, mask, besti, bestj);  // negative sums (SRGB) or DXT1 transparent texels
 }
 
 // reduce_colors_inplace_2fixpoints (s2tc_algorithm.cpp:415-478) for n = m = 16
@@ -168,7 +205,7 @@ __device__ __forceinline__ void reduce16_alpha(const int* ain, Scratch16& sc, in
 #pragma unroll
       for (int j = i + 1; j < 16; ++j, ++p) S[p] += wk * min(col[i], col[j]);
   }
-  pick_pair(S, 0xFFFFu, besti, bestj);
+  pick_pair_nonneg(S, besti, bestj);  // sums of squares: never negative
 }
 
 // ------------------------------------------------------------------------
@@ -351,6 +388,10 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
     if constexpr (FULL16) {
       int bi, bj;
       reduce16_rgb(tp, input_mask<DXT>(bt), sc, bi, bj);
+      // read by a run-time index, which places the block's texel words in
+      // local memory while the searches hold their sums in registers; keeping
+      // them in registers (selected by masks) or parking them in shared memory
+      // and reading them back measured 10% and 2.5% slower
       c0 = texel_c3(bt.px[(bi & 3) * 4 + (bi >> 2)]);
       c1 = texel_c3(bt.px[(bj & 3) * 4 + (bj >> 2)]);
       if (DXT == DXT5) {
@@ -531,6 +572,9 @@ __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
   if (!resolve(w, (long long)blockIdx.x * blockDim.x + threadIdx.x, a, bl)) return;
   const long long b = (long long)a.by0 * a.bw + bl;                         // block within the image
   const int by = int(b / a.bw), bx = int(b % a.bw);
+  // whole DXT3/DXT5 blocks of the all-texels mode belong to k_encode_full16:
+  // leave them without reading their texels
+  if (NORMAL && a.nrandom <= 0 && DXT != DXT1 && a.width - bx * 4 >= 4 && a.height - by * 4 >= 4) return;
   BlockTexels bt;
   load_block(a.t565, a.width, a.height, bx, by, bt);
   if (NORMAL && a.nrandom <= 0 && is_full<DXT>(bt)) return;
