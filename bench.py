@@ -55,6 +55,8 @@ WORKLOADS = {
         w=4096, h=4096, sc=4, fmt=0x83F3, dither=2, metric=3, nrandom=0, refine=2, gen="value_noise", seed=2),
     "plain_1024_dxt1_wavg_quick_always": dict(
         w=1024, h=1024, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
+    "plain_4096_dxt1_wavg_quick_always": dict(
+        w=4096, h=4096, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
     "plain_8192_dxt1_wavg_quick_always": dict(
         w=8192, h=8192, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="plain", seed=1),
     "normal_map_2048_dxt1_normalmap_rand64_loop": dict(
@@ -78,6 +80,11 @@ WORKLOADS = {
     "from_s3tc_8192_dxt5": dict(w=8192, h=8192, sc=4, fmt=0x83F3, gen="tool", tool="from_s3tc", seed=7),
     "dds_4096_dxt1_wavg_quick_always": dict(w=4096, h=4096, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1,
                                             gen="tool", tool="dds", seed=1),
+    # latency of one synchronous tx_compress_dxtn call on small images with the
+    # default knobs (pageable buffers, as a GL driver passes them)
+    "small_calls_dxt1_wavg_quick_always": dict(
+        w=0, h=0, sc=4, fmt=0x83F1, dither=1, metric=5, nrandom=-1, refine=1, gen="small", seed=3,
+        sizes=[64, 128, 256, 512, 1024]),
     # requests of log-uniform size 64..4096, DXT1/DXT5, WAVG/SRGB_MIXED/NORMALMAP,
     # through the continuous-batching request loop under a 32 GB budget; a
     # step is 1000 requests
@@ -179,6 +186,10 @@ def config_dict(wl_name: str, wl: dict) -> dict:
                 "height": wl["h"], "srccomps": 3, "format": "DXT1", "dither": s2.DITHER_NAMES[wl["dither"]],
                 "colordist": "NORMALMAP", "random_colors": wl["nrandom"], "refine": s2.REFINE_NAMES[wl["refine"]],
                 "l2": "the batch's inputs (805 MB) and rand words (13 GB) exceed the 129 MB L2"}
+    if wl["gen"] == "small":
+        return {"workload": wl_name, "sizes": [f"{n}x{n}" for n in wl["sizes"]], "srccomps": 4, "format": "DXT1",
+                "dither": "SIMPLE", "colordist": "WAVG", "random_colors": -1, "refine": "ALWAYS",
+                "entry": "tx_compress_dxtn, pageable host buffers", "l2": "small images: L2-resident by design"}
     if wl["gen"] == "serving":
         return {"workload": wl_name, "requests_per_step": wl["per_step"], "sizes": "log-uniform 64..4096 per side",
                 "formats": "DXT1/DXT5 uniform", "colordist": "WAVG/SRGB_MIXED/NORMALMAP uniform",
@@ -1018,6 +1029,57 @@ def run_serving_workload(args, wl_name: str, wl: dict) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ small calls
+
+def run_small_calls(args, wl_name: str, wl: dict) -> None:
+    """Per-call latency of tx_compress_dxtn on small square images (the cost a
+    GL driver sees per texture upload): pageable numpy buffers, one call after
+    another, host wall clock per call; each size checked against the oracle
+    once.  `value` is the texels/s of the largest size's calls."""
+    import torch
+    import s2tc_gb300 as s2
+    from s2tc_gb300 import workloads
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    oracle = pyoracle.Oracle()
+    lib = s2.load()
+    s2.set_env(wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+    l0 = s2.kernel_launches()
+    sizes, exact, launches = {}, True, {}
+    with ClockSampler(0) as clk:
+        for n in wl["sizes"]:
+            img = np.ascontiguousarray(workloads.plain_rgba(wl["seed"], n, n).reshape(-1))
+            out = np.zeros(s2.compressed_size(n, n, wl["fmt"]), np.uint8)
+            for _ in range(max(args.warmup, 3) * 10):
+                lib.tx_compress_dxtn(4, n, n, img.ctypes.data, wl["fmt"], out.ctypes.data, 0)
+            want = oracle.compress(4, n, n, img, wl["fmt"], wl["dither"], wl["metric"], wl["nrandom"], wl["refine"])
+            exact &= bool(np.array_equal(out, want))
+            calls = max(20, args.steps * 10)
+            k0 = s2.kernel_launches()
+            ts = []
+            for _ in range(calls):
+                t0 = time.perf_counter()
+                lib.tx_compress_dxtn(4, n, n, img.ctypes.data, wl["fmt"], out.ctypes.data, 0)
+                ts.append(time.perf_counter() - t0)
+            launches[f"{n}x{n}"] = (s2.kernel_launches() - k0) / calls
+            ts = np.array(ts) * 1e6
+            sizes[f"{n}x{n}"] = {"median_us": float(np.median(ts)), "p10_us": float(np.percentile(ts, 10)),
+                                 "p90_us": float(np.percentile(ts, 90)), "calls": calls}
+    big = f"{wl['sizes'][-1]}x{wl['sizes'][-1]}"
+    value = wl["sizes"][-1] ** 2 / (sizes[big]["median_us"] * 1e-6)
+    line = {"metric": METRIC, "value": value, "unit": "texels/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sizes[big]["median_us"] / 1000, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": dict(config_dict(wl_name, wl), sizes=wl["sizes"]),
+            "latency_per_call": sizes, "kernel_launches_per_call": launches, "bit_exact_vs_oracle": exact,
+            "e2e": {"value": value, "unit": "texels/s", "h2d_bytes_per_step": wl["sizes"][-1] ** 2 * 4,
+                    "d2h_bytes_per_step": s2.compressed_size(wl["sizes"][-1], wl["sizes"][-1], wl["fmt"]),
+                    "note": "pageable host buffers; one synchronous call per step"},
+            "gpu_launches": int(round(launches[big] * (max(20, args.steps * 10)))),
+            "roofline": None, "cpu_baseline": None, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------- multi-rank
 
 def aggregate_ranks(seconds: float, units: int, dist=None, device: str = "cpu"):
@@ -1054,7 +1116,7 @@ def main() -> None:
         if wl["gen"] in ("mips", "normal_batch"):
             run_reference_arm_batch(args, args.workload, wl)
             return
-        if wl["gen"] in ("serving", "tool"):
+        if wl["gen"] in ("serving", "tool", "small"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the encoder workloads"}))
             return
         run_reference_arm(args, args.workload, wl)
@@ -1067,6 +1129,9 @@ def main() -> None:
         return
     if wl["gen"] == "tool":
         run_tool_workload(args, args.workload, wl)
+        return
+    if wl["gen"] == "small":
+        run_small_calls(args, args.workload, wl)
         return
 
     import torch

@@ -8,6 +8,8 @@
 // points report the error and write nothing.
 #include "s2tc_gb300.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <strings.h>
 
@@ -40,6 +42,8 @@ bool cuda_ok(cudaError_t e, const char* what) {
   set_error(std::string(what) + ": " + cudaGetErrorString(e));
   return false;
 }
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Grow-only device buffer.
 struct DevBuf {
@@ -113,6 +117,8 @@ struct Context {
     return true;
   }
   PinnedBuf host_rnd, host_out;
+  DevBuf small_dev;      // small quick-mode calls: pixels, scan state, flag, blocks
+  PinnedBuf small_host;  // ... and their pinned mirror
   PinnedBuf host_flag;  // where the timeout flag is read back to
 
   bool init() {
@@ -287,6 +293,69 @@ int encode_locked(Context& c, const uint32_t* t565, int width, int height, int d
   return ST_OK;
 }
 
+// The strip kernel's view of an RGBA8 source for its TMA copies: the image
+// as a 2-D tensor of rows of 256 texels (32-bit words), texels / 256 rows of
+// 1024 bytes, one row per copy.  False (vector loads instead) for a source
+// that is not 16-byte aligned, an image under 256 texels, or a driver without
+// the tensor-map entry point.
+bool rgba_rows_map(const void* src, long long npx, CUtensorMap* map, long long* rows) {
+  if ((reinterpret_cast<uintptr_t>(src) & 15) != 0 || npx < 256) return false;
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return PFN_cuTensorMapEncodeTiled_v12000(nullptr);
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
+  const cuuint64_t dims[2] = {256, cuuint64_t(npx / 256)};
+  const cuuint64_t strides[1] = {1024};
+  const cuuint32_t box[2] = {256, 1};
+  const cuuint32_t elem[2] = {1, 1};
+  if (encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(src), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  *rows = npx / 256;
+  return true;
+}
+
+// The quick mode (darkest/brightest selection) with NONE or SIMPLE dither on
+// images up to kStripMaxWidth texels wide runs as one fused strip kernel.
+bool strip_mode(const s2tc_options& opt, int width, int height, StripPlan* plan) {
+#ifdef S2TC_STRIP_OFF
+  return false;  // build-time switch: the two-kernel path only (for comparisons)
+#endif
+  return !normal_mode(opt) && opt.dither != DI_FLOYDSTEINBERG && strip_plan(width, height, *plan);
+}
+
+// Arguments of a strip launch over the whole image.
+StripArgs strip_args(const StripPlan& plan, int sc, int width, int height, const uint8_t* d_src, int dxt, int dither,
+                     uint8_t* d_dst, long long pitch, int* error) {
+  StripArgs a{};
+  a.src = d_src;
+  a.width = width;
+  a.height = height;
+  a.srccomps = sc;
+  a.alphabits = alpha_bits(dxt);
+  a.dither = dither == DI_NONE ? DI_NONE : DI_SIMPLE;
+  a.dst = d_dst;
+  a.pitch = pitch;
+  const int bs = block_bytes(dxt);
+  a.aligned = ((reinterpret_cast<uintptr_t>(d_dst) % bs) == 0 && (pitch % bs) == 0) ? 1 : 0;
+  a.seg = plan.seg;
+  a.rows_per_band = plan.rows_per_band;
+  a.band_base = 0;
+  a.nbands = plan.bands;
+  a.image_bands = plan.bands;
+  a.scan.error = error;
+  return a;
+}
+
 // `carry` (device int, may be null): the second alpha endpoint that the
 // previous call's last block left behind.  The reference encodes every block
 // of every call in the same stack frame, and a DXT5 image whose first block
@@ -299,6 +368,27 @@ int compress_device_locked(Context& c, int srccomps, int width, int height, cons
                            cudaStream_t s, int* carry = nullptr) {
   const int sc = srccomps == 3 ? 3 : 4;
   const long long npx = (long long)width * height;
+  StripPlan plan;
+  if (strip_mode(opt, width, height, &plan)) {
+    // one fused launch: the texel words stay in shared memory
+    if (!c.scratch.reserve(dither_batch_scratch_bytes(plan.bands), "cudaMalloc(scratch)")) return ST_OUT_OF_MEMORY;
+    if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return ST_CUDA_ERROR;
+    StripArgs sa = strip_args(plan, sc, width, height, d_src, dxt, opt.dither, d_dst, pitch, c.err.as<int>());
+    CUtensorMap map;
+    sa.use_tma = sc == 4 && rgba_rows_map(d_src, npx, &map, &sa.tma_rows);
+    cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
+    // the stage timing puts the fused kernel under "encode"
+    if (tev && (!cuda_ok(cudaEventRecord(tev[0], s), "cudaEventRecord") ||
+                !cuda_ok(cudaEventRecord(tev[1], s), "cudaEventRecord")))
+      return ST_CUDA_ERROR;
+    if (!cuda_ok(launch_strip(sa, &map, dxt, opt.metric, opt.refine, c.scratch.as<uint8_t>(), s), "strip launch"))
+      return ST_CUDA_ERROR;
+    if (tev) {
+      if (!cuda_ok(cudaEventRecord(tev[2], s), "cudaEventRecord")) return ST_CUDA_ERROR;
+      c.timed_calls++;
+    }
+    return cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord") ? ST_OK : ST_CUDA_ERROR;
+  }
   if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return ST_OUT_OF_MEMORY;
   size_t scratch = dither_scratch_bytes(npx);
   if (opt.dither == DI_FLOYDSTEINBERG) scratch = dither_fs_scratch_bytes(width, height);
@@ -383,11 +473,80 @@ constexpr long long kPipeTargetRanges = 12;
 // ranges = ceil(tiles / per_range) <= kPipeTargetRanges, as per_range >= ceil(tiles / kPipeTargetRanges)
 static_assert(kPipeTargetRanges <= Context::kPipeRanges, "one event set per range");
 
+// The same for the fused strip kernel (quick mode): the image goes up in
+// ranges of bands on the copy stream, one strip launch per range on the
+// compute stream (its look-back reaches into the ranges before it), and each
+// range's block rows come back on the second copy stream when `dest` is
+// pinned.
+bool compress_host_pipelined_strip(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
+                                   unsigned char* dest, long long diff, const s2tc_options& opt,
+                                   const StripPlan& plan) {
+  cudaStream_t s = c.stream;
+  const long long npx = (long long)width * height;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const long long row_bytes = (long long)bw * block_bytes(dxt);
+  const long long band_texels = 4ll * plan.rows_per_band * width;
+  const long long min_bands = std::max(1ll, (kPipeRangeTiles * dither_tile_texels() + band_texels - 1) / band_texels);
+  const long long per_range = std::max(min_bands, (plan.bands + kPipeTargetRanges - 1) / kPipeTargetRanges);
+  const int ranges = int((plan.bands + per_range - 1) / per_range);
+  if (!c.src.reserve(size_t(npx) * sc + 16, "cudaMalloc(src)")) return true;
+  if (!c.dst.reserve(size_t(row_bytes) * bh + 16, "cudaMalloc(dst)")) return true;
+  if (!c.scratch.reserve(dither_batch_scratch_bytes(plan.bands), "cudaMalloc(scratch)")) return true;
+  if (!cuda_ok(cudaStreamWaitEvent(s, c.arena_free, 0), "cudaStreamWaitEvent")) return true;
+  if (!cuda_ok(cudaStreamWaitEvent(c.copy_in, c.arena_free, 0), "cudaStreamWaitEvent")) return true;
+  const bool pinned_out = host_pinned(dest);
+  uint8_t* d_src = c.src.as<uint8_t>();
+  uint8_t* d_dst = c.dst.as<uint8_t>();
+  StripArgs sa = strip_args(plan, sc, width, height, d_src, dxt, opt.dither, d_dst, row_bytes, c.err.as<int>());
+  CUtensorMap map;
+  sa.use_tma = sc == 4 && rgba_rows_map(d_src, npx, &map, &sa.tma_rows);
+  for (int r = 0; r < ranges; ++r) {
+    const long long b0 = r * per_range, b1 = std::min(plan.bands, b0 + per_range);
+    const long long p0 = b0 * band_texels, p1 = std::min(npx, b1 * band_texels);
+    const int y0 = int(b0 * plan.rows_per_band), y1 = int(std::min<long long>(bh, b1 * plan.rows_per_band));
+    sa.band_base = b0;
+    sa.nbands = b1 - b0;
+    if (!cuda_ok(cudaMemcpyAsync(d_src + p0 * sc, src + p0 * sc, size_t(p1 - p0) * sc, cudaMemcpyHostToDevice,
+                                 c.copy_in),
+                 "input upload") ||
+        !cuda_ok(cudaEventRecord(c.pipe_in[r], c.copy_in), "cudaEventRecord") ||
+        !cuda_ok(cudaStreamWaitEvent(s, c.pipe_in[r], 0), "cudaStreamWaitEvent") ||
+        !cuda_ok(launch_strip(sa, &map, dxt, opt.metric, opt.refine, c.scratch.as<uint8_t>(), s), "strip launch"))
+      return true;
+    if (pinned_out) {
+      if (!cuda_ok(cudaEventRecord(c.pipe_out[r], s), "cudaEventRecord") ||
+          !cuda_ok(cudaStreamWaitEvent(c.copy_out, c.pipe_out[r], 0), "cudaStreamWaitEvent") ||
+          !cuda_ok(cudaMemcpy2DAsync(dest + (long long)y0 * (row_bytes + diff), size_t(row_bytes + diff),
+                                     d_dst + (long long)y0 * row_bytes, size_t(row_bytes), size_t(row_bytes),
+                                     size_t(y1 - y0), cudaMemcpyDeviceToHost, c.copy_out),
+                   "output download"))
+        return true;
+    }
+  }
+  if (!pinned_out &&
+      !cuda_ok(cudaMemcpy2DAsync(dest, size_t(row_bytes + diff), d_dst, size_t(row_bytes), size_t(row_bytes),
+                                 size_t(bh), cudaMemcpyDeviceToHost, s),
+               "output download"))
+    return true;
+  if (!cuda_ok(cudaEventRecord(c.pipe_out[0], c.copy_out), "cudaEventRecord") ||
+      !cuda_ok(cudaStreamWaitEvent(s, c.pipe_out[0], 0), "cudaStreamWaitEvent") ||
+      !cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord"))
+    return true;
+  check_error_flag(c, s);
+  return true;
+}
+
 bool compress_host_pipelined(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                              unsigned char* dest, long long diff, const s2tc_options& opt, bool* done) {
   *done = false;
   const long long npx = (long long)width * height;
   if (npx < kPipeMinTexels || opt.dither == DI_FLOYDSTEINBERG || diff < 0) return false;
+  StripPlan plan;
+  if (strip_mode(opt, width, height, &plan)) {
+    if (!c.init_pipe()) return false;
+    *done = true;
+    return compress_host_pipelined_strip(c, sc, width, height, src, dxt, dest, diff, opt, plan);
+  }
   const bool normal = normal_mode(opt);
   const int per_block = rand_per_block(opt, dxt);
   if (per_block > 0 && !rand_usable()) return false;
@@ -508,6 +667,76 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   return true;
 }
 
+// Small images in the quick mode: one fused launch between one upload and one
+// download.  A device arena holds [pixels | ticket | status words | flag |
+// blocks | aggregate records] and a pinned buffer mirrors its first part:
+// the upload carries the pixels and the zeroed ticket, status words and
+// timeout flag, the download brings back the flag and the blocks.  Four CUDA
+// calls per image (upload, launch, download, wait) instead of about ten: a
+// 64x64 call measured 29.5 us instead of 50 us, 256x256 43 us instead of
+// 72 us.  Larger images take the ordinary path: past about 64 Ki texels the
+// host copies through the staging buffer cost more than the calls they save
+// (1024x1024: 348 us against 96 us).
+constexpr long long kSmallCallTexels = 1ll << 16;
+
+bool compress_host_small(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
+                         unsigned char* dest, int dstRowStride, const s2tc_options& opt, bool* done) {
+  *done = false;
+  const long long npx = (long long)width * height;
+  StripPlan plan;
+  if (npx > kSmallCallTexels || !strip_mode(opt, width, height, &plan)) return false;
+  *done = true;
+  const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
+  const size_t row_bytes = size_t(bw) * bs, out_bytes = row_bytes * bh;
+  const size_t o_ticket = align_up(size_t(npx) * sc, 256), o_status = o_ticket + 16;
+  const size_t o_flag = align_up(o_status + size_t(plan.bands) * 8, 16), o_blocks = o_flag + 16;
+  const size_t o_aggs = align_up(o_blocks + out_bytes, 16), total = o_aggs + size_t(plan.bands) * 72;
+  if (!c.small_dev.reserve(total, "cudaMalloc(small call)") ||
+      !c.small_host.reserve(o_blocks + out_bytes, "cudaMallocHost(small call)"))
+    return true;
+  uint8_t* h = static_cast<uint8_t*>(c.small_host.p);
+  uint8_t* d = c.small_dev.as<uint8_t>();
+  std::memcpy(h, src, size_t(npx) * sc);
+  std::memset(h + o_ticket, 0, o_blocks - o_ticket);
+  StripArgs sa = strip_args(plan, sc, width, height, d, dxt, opt.dither, d + o_blocks, (long long)row_bytes,
+                            reinterpret_cast<int*>(d + o_flag));
+  sa.scan.ticket = reinterpret_cast<unsigned int*>(d + o_ticket);
+  sa.scan.status = reinterpret_cast<unsigned long long*>(d + o_status);
+  sa.scan.aggs = d + o_aggs;
+  CUtensorMap map;
+  sa.use_tma = sc == 4 && rgba_rows_map(d, npx, &map, &sa.tma_rows);
+  cudaStream_t s = c.stream;
+  cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
+  if (!cuda_ok(cudaMemcpyAsync(d, h, o_blocks, cudaMemcpyHostToDevice, s), "input upload")) return true;
+  if (tev && (!cuda_ok(cudaEventRecord(tev[0], s), "cudaEventRecord") ||
+              !cuda_ok(cudaEventRecord(tev[1], s), "cudaEventRecord")))
+    return true;
+  if (!cuda_ok(launch_strip(sa, &map, dxt, opt.metric, opt.refine, nullptr, s), "strip launch")) return true;
+  if (tev) {
+    if (!cuda_ok(cudaEventRecord(tev[2], s), "cudaEventRecord")) return true;
+    c.timed_calls++;
+  }
+  if (!cuda_ok(cudaMemcpyAsync(h + o_flag, d + o_flag, 16 + out_bytes, cudaMemcpyDeviceToHost, s), "output download") ||
+      !cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize"))
+    return true;
+  if (*reinterpret_cast<const int*>(h + o_flag)) {
+    set_error("a bounded wait in the dither scan gave up");
+    return true;
+  }
+  // output rows: packed, or dstRowStride apart (s2tc_libtxc_dxtn.cpp:243, 261, 279); a stride below
+  // the padded row overlaps rows, later rows overwriting the end of earlier ones
+  const long long diff =
+      dstRowStride >= width * (bs / 4) ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs / 4) : 0;
+  const uint8_t* blocks = h + o_blocks;
+  if (diff == 0) {
+    std::memcpy(dest, blocks, out_bytes);
+  } else {
+    for (int r = 0; r < bh; ++r)
+      std::memmove(dest + r * (long long)(row_bytes + diff), blocks + r * row_bytes, row_bytes);
+  }
+  return true;
+}
+
 // Host-memory compression used by tx_compress_dxtn.
 void compress_host(int srccomps, int width, int height, const unsigned char* src, int dxt, unsigned char* dest,
                    int dstRowStride, const s2tc_options& opt) {
@@ -515,6 +744,11 @@ void compress_host(int srccomps, int width, int height, const unsigned char* src
   std::lock_guard<std::mutex> lock(c.mu);
   if (!c.init()) return;
   cudaStream_t s = c.stream;
+  {
+    bool done = false;
+    compress_host_small(c, srccomps == 3 ? 3 : 4, width, height, src, dxt, dest, dstRowStride, opt, &done);
+    if (done) return;
+  }
   {
     const int bs0 = block_bytes(dxt);
     const long long diff0 = dstRowStride >= width * (bs0 / 4)
@@ -620,7 +854,6 @@ struct Batch {
   }
 };
 
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Lay out, allocate and upload everything a batch's launches need.
 int batch_prepare(Batch& b, Context& c) {

@@ -58,6 +58,8 @@ struct DitherWork {
 // `spin_limit` polls (0: the default limit).  The tiles behind a held tile
 // time out, set the error flag and finish; the call reports S2TC_ERR_TIMEOUT.
 void set_dither_test_hold(long long hold_tile, int spin_limit);
+// The values set_dither_test_hold set last (for other kernels that run the scan).
+void dither_test_hold_values(long long* hold_tile, int* spin_limit);
 
 // Texels per tile of the batched/SIMPLE dither kernels.
 long long dither_tile_texels();

@@ -11,8 +11,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
+
+#include <cuda.h>
 
 #include "dither.h"
+#include "dither_scan.cuh"
 #include "encode.h"
 #include "s2tc_device.cuh"
 
@@ -349,7 +353,7 @@ __device__ __forceinline__ bool is_full(const BlockTexels& bt) {
 // random candidates); the return value is this block's leftover for the next.
 template <int DXT, bool NORMAL, int REFINE, bool FULL16>
 __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* rnd, int prev_a1,
-                            EncodedBlock& out, Scratch16& sc) {
+                            EncodedBlock& out, Scratch16* sc) {
   constexpr bool TRANS = DXT == DXT1;
   P tp[16];
 #pragma unroll
@@ -387,7 +391,7 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
   } else {
     if constexpr (FULL16) {
       int bi, bj;
-      reduce16_rgb(tp, input_mask<DXT>(bt), sc, bi, bj);
+      reduce16_rgb(tp, input_mask<DXT>(bt), *sc, bi, bj);
       // read by a run-time index, which places the block's texel words in
       // local memory while the searches hold their sums in registers; keeping
       // them in registers (selected by masks) or parking them in shared memory
@@ -398,7 +402,7 @@ __device__ int encode_block(const BlockTexels& bt, int nrandom, const uint32_t* 
         int ain[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) ain[k] = texel_a(bt.px[in_slot(k)]);
-        reduce16_alpha(ain, sc, bi, bj);
+        reduce16_alpha(ain, *sc, bi, bj);
         a0 = texel_a(bt.px[(bi & 3) * 4 + (bi >> 2)]);
         a1 = texel_a(bt.px[(bj & 3) * 4 + (bj >> 2)]);
       }
@@ -556,7 +560,7 @@ __global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encod
   load_block(a.t565, a.width, a.height, bx, by, bt);
   if (!is_full<DXT>(bt)) return;  // left to k_encode
   EncodedBlock eb;
-  const int leftover = encode_block<DXT, true, REFINE, true>(bt, 0, nullptr, -1, eb, sc);
+  const int leftover = encode_block<DXT, true, REFINE, true>(bt, 0, nullptr, -1, eb, &sc);
   if (a.leftover_out && b == (long long)a.bw * a.bh - 1) *a.leftover_out = leftover;
   store_block(a, DXT, bx, by, eb);
 }
@@ -566,7 +570,6 @@ __global__ void __launch_bounds__(kThreadsPerCta, S2TC_FULL16_MINBLOCKS) k_encod
 // candidates the full blocks are skipped (k_encode_full16 encodes them).
 template <int DXT, bool NORMAL, int REFINE>
 __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
-  __shared__ Scratch16 sc;
   EncodeArgs a;
   long long bl;  // block within this launch's part of the image
   if (!resolve(w, (long long)blockIdx.x * blockDim.x + threadIdx.x, a, bl)) return;
@@ -592,13 +595,13 @@ __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
       BlockTexels pt;
       load_block(a.t565, a.width, a.height, pbx, pby, pt);
       EncodedBlock scratch;
-      prev_a1 = encode_block<DXT, NORMAL, REFINE, false>(pt, a.nrandom, nullptr, -1, scratch, sc);
+      prev_a1 = encode_block<DXT, NORMAL, REFINE, false>(pt, a.nrandom, nullptr, -1, scratch, nullptr);
     } else {
       prev_a1 = a.prev_a1_dev ? *a.prev_a1_dev : a.prev_a1_first;
     }
   }
   EncodedBlock eb;
-  const int leftover = encode_block<DXT, NORMAL, REFINE, false>(bt, a.nrandom, rnd, prev_a1, eb, sc);
+  const int leftover = encode_block<DXT, NORMAL, REFINE, false>(bt, a.nrandom, rnd, prev_a1, eb, nullptr);
   if (a.leftover_out && b == (long long)a.bw * a.bh - 1) *a.leftover_out = leftover;
   store_block(a, DXT, bx, by, eb);
 }
@@ -1302,10 +1305,213 @@ cudaError_t launch_d(const EncodeWork& a, bool normal, int refine, cudaStream_t 
   return launch_r<DXT, (kMetric == CD_NORMALMAP)>(a, refine, s);
 }
 
+// ------------------------------------------------------------------------
+// Fused strip kernel of the quick mode: the NONE or SIMPLE dither and the
+// quick encoder (darkest/brightest selection) in one launch.
+//
+// A CTA takes a band of whole block rows, i.e. one contiguous raster range of
+// the image: 4 * rows_per_band texel rows.  RGBA8 sources come in by the TMA
+// unit: the image seen as a 2-D tensor of rows of 256 texels (one 32-bit word
+// each), one cp.async.bulk.tensor copy per row, issued by the 32 lanes of warp
+// 0 and completing on one mbarrier.  The inner coordinate is always 0, so
+// every copy starts on a 16-byte boundary; the band begins `p0 % 256` words
+// into the first row, and the texels after the last whole row of the image
+// come in by plain loads.  Other sources (RGB8, unaligned) take vector loads.
+// The band's SIMPLE scan is the dither kernel's (dither_scan.cuh), chained
+// to the bands before it by the same decoupled look-back; its 5:6:5 words
+// stay in shared memory, where the band's blocks are read and encoded, one
+// thread per block, and written out in block order.  HBM then sees the
+// source once and the blocks once.
+
+constexpr int kStripPad = 512;  // words before the band: its offset in the first tensor row, and the last row's rest
+template <int SEG>
+using StripSmem = ScanSmem<kStripThreads, SEG, kStripPad>;
+
+__device__ __forceinline__ void tma_row(uint32_t dst, const CUtensorMap* map, int row, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(row), "r"(mbar)
+      : "memory");
+}
+
+// RGBA word of texel i of a packed RGBA8 image.
+__device__ __forceinline__ uint32_t rgba_word(const uint8_t* src, long long i) {
+  const uint8_t* b = src + 4 * i;
+  if ((reinterpret_cast<uintptr_t>(b) & 3) == 0) return __ldg(reinterpret_cast<const uint32_t*>(b));
+  return uint32_t(b[0]) | (uint32_t(b[1]) << 8) | (uint32_t(b[2]) << 16) | (uint32_t(b[3]) << 24);
+}
+
+// Two CTAs per SM (128 registers); three (85 registers, with spills) measured
+// the same.
+template <int DXT, int REFINE, int SEG>
+__global__ void __launch_bounds__(kStripThreads, 2) k_strip_quick(const __grid_constant__ CUtensorMap tmap,
+                                                                  StripArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  StripSmem<SEG>& sm =
+      *reinterpret_cast<StripSmem<SEG>*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  __shared__ unsigned int s_ticket;
+  const int t = threadIdx.x;
+  init_tables(sm);
+  if (t == 0) s_ticket = atomicAdd(a.scan.ticket, 1u);
+  bulk_init(sm);
+  __syncthreads();
+  if ((long long)s_ticket >= a.nbands) return;
+  const long long band = a.band_base + s_ticket;
+  const int W = a.width, H = a.height, bw = (W + 3) / 4, bh = (H + 3) / 4;
+  const int by0 = int(band * a.rows_per_band);
+  const int nby = min(a.rows_per_band, bh - by0);
+  const int rows = min(4 * nby, H - 4 * by0);
+  const long long p0 = (long long)by0 * 4 * W;
+  const int n = rows * W;
+  uint32_t* base = sm.px;
+  if (a.use_tma) {
+    base = sm.px + int(p0 & 255);
+    const long long row0 = p0 >> 8;
+    const long long covered = a.tma_rows << 8;  // texels inside the tensor
+    const long long end = min(p0 + n, covered);
+    const int nrows = end > (row0 << 8) ? int((end - (row0 << 8) + 255) >> 8) : 0;
+    const uint32_t mbar = smem_u32(&sm.mbar);
+    if (t < 32) {
+      if (t == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(uint32_t(nrows) * 1024u)
+                     : "memory");
+      __syncwarp();
+      for (int r = t; r < nrows; r += 32) tma_row(smem_u32(sm.px + r * 256), &tmap, int(row0 + r), mbar);
+    }
+    int spins = 0;
+    while (!mbar_try_wait(mbar, 0) && ++spins < kBulkSpins) {
+    }
+    // one decision for the whole CTA (the branch below has a barrier)
+    if (__syncthreads_or(spins >= kBulkSpins)) {
+      // the copies did not complete within the bounded wait: the call reports
+      // S2TC_ERR_TIMEOUT (output undefined); the band goes on with plain loads
+      // after a second bounded wait, so that the bands behind it do not wait
+      // out their own limits
+      if (t == 0) atomicExch(a.scan.error, 1);
+      bulk_load_wait(sm);
+      __syncthreads();
+      for (int i = t; i < n; i += kStripThreads) base[i] = rgba_word(a.src, p0 + i);
+    }
+    for (long long i = max(p0, covered) - p0 + t; i < n; i += kStripThreads) base[i] = rgba_word(a.src, p0 + i);
+  } else {
+    load_tile<kStripThreads>(DitherItem{a.src, W, H, a.srccomps, a.alphabits, nullptr}, p0, n, base);
+  }
+  __syncthreads();
+  if (a.dither == DI_SIMPLE) {
+    if (a.srccomps == 3) simple_tile<0>(a.alphabits, band, band, n, a.scan, sm, base);
+    else if (a.alphabits == 1) simple_tile<1>(a.alphabits, band, band, n, a.scan, sm, base);
+    else if (a.alphabits == 4) simple_tile<4>(a.alphabits, band, band, n, a.scan, sm, base);
+    else simple_tile<8>(a.alphabits, band, band, n, a.scan, sm, base);
+  } else {
+    // DITHER_NONE (s2tc_algorithm.cpp:1269-1305): plain truncation
+    const uint32_t ac = uint32_t((1 << a.alphabits) - 1);
+    const int ash = 8 - a.alphabits;
+    for (int i = t; i < n; i += kStripThreads) {
+      const uint32_t q = base[i];
+      const uint32_t al = a.srccomps == 3 ? ac : (q >> 24) >> ash;
+      base[i] = ((q & 0xFFu) >> 3) | ((((q >> 8) & 0xFFu) >> 2) << 8) | ((((q >> 16) & 0xFFu) >> 3) << 16) | (al << 24);
+    }
+  }
+  __syncthreads();
+  // the band's blocks, one thread per block, in block order
+  const bool vec = (W & 3) == 0;
+  for (int k = t; k < nby * bw; k += kStripThreads) {
+    const int ly = k / bw, bx = k - ly * bw;
+    BlockTexels bt;
+    bt.w = min(4, W - 4 * bx);
+    bt.h = min(4, rows - 4 * ly);
+    const uint32_t* q = base + 4 * ly * W + 4 * bx;
+    if (vec && bt.w == 4 && bt.h == 4) {
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const uint4 v = *reinterpret_cast<const uint4*>(q + y * W);
+        bt.px[y * 4 + 0] = v.x;
+        bt.px[y * 4 + 1] = v.y;
+        bt.px[y * 4 + 2] = v.z;
+        bt.px[y * 4 + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int y = 0; y < 4; ++y)
+#pragma unroll
+        for (int x = 0; x < 4; ++x) bt.px[y * 4 + x] = (x < bt.w && y < bt.h) ? q[y * W + x] : 0u;
+    }
+    EncodedBlock eb;
+    encode_block<DXT, false, REFINE, false>(bt, -1, nullptr, -1, eb, nullptr);
+    uint8_t* o = a.dst + (size_t)(by0 + ly) * a.pitch + (size_t)bx * (DXT == DXT1 ? 8 : 16);
+    if (a.aligned) {
+      if (DXT == DXT1) *reinterpret_cast<uint64_t*>(o) = eb.lo;
+      else *reinterpret_cast<ulonglong2*>(o) = make_ulonglong2(eb.lo, eb.hi);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) o[i] = uint8_t(eb.lo >> (8 * i));
+      if (DXT != DXT1) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) o[8 + i] = uint8_t(eb.hi >> (8 * i));
+      }
+    }
+  }
+}
+
+template <int DXT, int REFINE, int SEG>
+cudaError_t launch_strip_k(const StripArgs& a, const CUtensorMap& map, cudaStream_t s) {
+  const size_t smem = sizeof(StripSmem<SEG>) + 128;
+  static const cudaError_t attr = cudaFuncSetAttribute(k_strip_quick<DXT, REFINE, SEG>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (attr != cudaSuccess) return attr;
+  count_launches(1);
+  k_strip_quick<DXT, REFINE, SEG><<<unsigned(a.nbands), kStripThreads, smem, s>>>(map, a);
+  return cudaGetLastError();
+}
+
+template <int DXT, int REFINE>
+cudaError_t launch_strip_r(const StripArgs& a, const CUtensorMap& map, cudaStream_t s) {
+  return a.seg == 65 ? launch_strip_k<DXT, REFINE, 65>(a, map, s) : launch_strip_k<DXT, REFINE, 17>(a, map, s);
+}
+
+template <int DXT>
+cudaError_t launch_strip_d(const StripArgs& a, const CUtensorMap& map, int refine, cudaStream_t s) {
+  switch (refine) {
+    case RF_NEVER: return launch_strip_r<DXT, RF_NEVER>(a, map, s);
+    case RF_LOOP: return launch_strip_r<DXT, RF_LOOP>(a, map, s);
+    default: return launch_strip_r<DXT, RF_ALWAYS>(a, map, s);
+  }
+}
+
 }  // namespace
 
 #define S2TC_CAT2(a, b) a##b
 #define S2TC_CAT(a, b) S2TC_CAT2(a, b)
+
+cudaError_t S2TC_CAT(launch_strip_m, S2TC_METRIC)(StripArgs a, const void* tmap, int dxt, int refine,
+                                                  uint8_t* scratch, cudaStream_t s) {
+  // NORMALMAP never uses the quick selection (s2tc_algorithm.cpp:1127-1143)
+  if (kMetric == CD_NORMALMAP || a.nbands <= 0) return kMetric == CD_NORMALMAP ? cudaErrorNotSupported : cudaSuccess;
+  if (a.seg != 65 && a.seg != 17) return cudaErrorInvalidValue;
+  if (a.band_base < 0 || a.band_base + a.nbands > a.image_bands) return cudaErrorInvalidValue;
+  dither_test_hold_values(&a.scan.hold_tile, &a.scan.spin_limit);
+  if (scratch) {
+    // the layout of launch_dither_batch's scratch for image_bands tiles
+    a.scan.status = reinterpret_cast<unsigned long long*>(scratch);
+    a.scan.aggs = scratch + a.image_bands * sizeof(unsigned long long);
+    uintptr_t tk = reinterpret_cast<uintptr_t>(a.scan.aggs + a.image_bands * kRecWords * 4);
+    a.scan.ticket = reinterpret_cast<unsigned int*>((tk + 15) & ~uintptr_t(15));
+    cudaError_t e = cudaMemsetAsync(a.scan.status + a.band_base, 0, a.nbands * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.scan.ticket, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+  } else if (!a.scan.status || !a.scan.aggs || !a.scan.ticket || a.band_base != 0) {
+    return cudaErrorInvalidValue;
+  }
+  CUtensorMap map;
+  if (a.use_tma) map = *static_cast<const CUtensorMap*>(tmap);
+  else std::memset(&map, 0, sizeof(map));
+  switch (dxt) {
+    case DXT1: return launch_strip_d<DXT1>(a, map, refine, s);
+    case DXT3: return launch_strip_d<DXT3>(a, map, refine, s);
+    default: return launch_strip_d<DXT5>(a, map, refine, s);
+  }
+}
 
 cudaError_t S2TC_CAT(launch_encode_m, S2TC_METRIC)(const EncodeWork& a, int dxt, bool normal, int refine,
                                                    cudaStream_t s) {

@@ -4,6 +4,8 @@
 
 #include <cstdint>
 
+#include "dither.h"
+
 namespace s2tc {
 
 struct EncodeArgs {
@@ -36,6 +38,82 @@ struct EncodeWork {
   int nrandom;               // S2TC_RANDOM_COLORS of every image
   EncodeArgs single;
 };
+
+// Fused strip kernel of the quick mode (encode.cu, k_strip_quick): the NONE
+// or SIMPLE dither and the quick encoder in one launch, one CTA of 256
+// threads per band of `rows_per_band` whole block rows, the texel words kept
+// in shared memory.  A thread scans `seg` texels: 65, or 17 where 65 would
+// leave the GPU with fewer bands than it holds CTAs (small images: more,
+// shorter bands).  Rows of at most kStripMaxWidth texels; wider images take
+// the two kernels, which were faster there (a 512-thread variant for 8192-wide
+// rows ran 16% slower than the separate dither and encoder launches).
+constexpr int kStripThreads = 256;
+constexpr int kStripMaxWidth = kStripThreads * 65 / 4;  // 4160
+constexpr long long kStripFullBands = 2 * 152;          // bands that fill the GPU (two CTAs per SM)
+
+struct StripPlan {
+  int seg;            // texels per thread of the scan (17 or 65)
+  int rows_per_band;  // block rows per band
+  long long bands;
+};
+inline bool strip_plan(int width, int height, StripPlan& p) {
+  if (width <= 0 || height <= 0 || width > kStripMaxWidth) return false;
+  const long long four_w = 4ll * width, bh = (height + 3) / 4;
+  for (int seg : {65, 17}) {
+    if (four_w > kStripThreads * seg) break;
+    p.seg = seg;
+    p.rows_per_band = int(kStripThreads * seg / four_w);
+    p.bands = (bh + p.rows_per_band - 1) / p.rows_per_band;
+    if (p.bands >= kStripFullBands) break;
+  }
+  return true;
+}
+
+struct StripArgs {
+  const uint8_t* src;   // packed RGB8/RGBA8
+  int width, height, srccomps, alphabits;
+  int dither;           // DI_NONE or DI_SIMPLE
+  uint8_t* dst;         // first block
+  long long pitch;      // bytes between block rows
+  int aligned;          // dst and pitch allow 8/16-byte stores
+  int seg, rows_per_band;
+  long long band_base;  // bands [band_base, band_base + nbands) of the image
+  long long nbands;
+  long long image_bands;  // bands of the whole image (the scan state's layout)
+  int use_tma;          // RGBA8 rows through the tensor map (16-byte aligned source)
+  long long tma_rows;   // 256-texel rows the tensor map covers (texels / 256)
+  DitherWork scan;      // scan state: status, aggs, ticket (zeroed by the launcher), error
+};
+
+// Launches k_strip_quick over a.nbands bands; `scratch` holds
+// dither_batch_scratch_bytes(a.image_bands) (the launch zeroes the status
+// words of its bands and its ticket; ranges of one image launched in order
+// on one stream chain through it).  With `scratch` null the scan state is
+// a.scan.status / aggs / ticket as given, already zeroed by the caller (one
+// launch per image).  `tmap` is the CUtensorMap of
+// the source (ignored unless a.use_tma).  Returns cudaErrorNotSupported for a
+// metric without the quick selection (NORMALMAP).
+cudaError_t launch_strip_m0(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m1(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m2(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m3(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m4(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m5(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m6(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+cudaError_t launch_strip_m7(StripArgs, const void* tmap, int dxt, int refine, uint8_t* scratch, cudaStream_t);
+inline cudaError_t launch_strip(const StripArgs& a, const void* tmap, int dxt, int metric, int refine,
+                                uint8_t* scratch, cudaStream_t s) {
+  switch (metric) {
+    case 0: return launch_strip_m0(a, tmap, dxt, refine, scratch, s);
+    case 1: return launch_strip_m1(a, tmap, dxt, refine, scratch, s);
+    case 2: return launch_strip_m2(a, tmap, dxt, refine, scratch, s);
+    case 3: return launch_strip_m3(a, tmap, dxt, refine, scratch, s);
+    case 4: return launch_strip_m4(a, tmap, dxt, refine, scratch, s);
+    case 6: return launch_strip_m6(a, tmap, dxt, refine, scratch, s);
+    case 7: return launch_strip_m7(a, tmap, dxt, refine, scratch, s);
+    default: return launch_strip_m5(a, tmap, dxt, refine, scratch, s);
+  }
+}
 
 // Launch layout of the encoder kernels for one mode (the autotuner's knobs;
 // no effect on the bytes).

@@ -535,3 +535,61 @@ def test_pipelined_host_path(lib):
             assert np.array_equal(got, b), (sc, hex(fmt), stride)
         else:
             assert np.array_equal(a, b), (sc, hex(fmt), dither, metric, nr)
+
+
+# --------------------------------------------------------------- strip kernel
+# The quick mode with NONE or SIMPLE dither runs as one fused kernel over
+# bands of whole block rows (images up to 4160 texels wide): the scan's
+# chain crosses every band boundary, and RGBA8 sources come in by tensor
+# copies of 256-texel rows that start inside a band's first row.
+
+STRIP_SHAPES = [(3, 5), (255, 1), (257, 3), (1000, 77), (1001, 70), (4160, 9), (4161, 13), (1088, 300),
+                (1089, 301), (2000, 600), (64, 260), (130, 131), (4160, 1201), (1024, 1024)]
+
+
+@pytest.mark.parametrize("fmt", [0x83F1, 0x83F2, 0x83F3])
+def test_strip_bands_and_edges(lib, oracle, fmt):
+    """Widths around the band sizes, the 17- and 65-texel segments and the
+    4160 limit (4161 takes the two kernels), widths and heights that are not multiples of 4, RGB and RGBA,
+    NONE and SIMPLE dither, every refinement, against the oracle."""
+    rng = np.random.default_rng(fmt)
+    for k, (w, h) in enumerate(STRIP_SHAPES):
+        sc = 4 if k % 2 == 0 else 3
+        img = cases.image(rng, w, h, sc, kind=[0, 4, 2, 0][k % 4])
+        dither, metric, refine = k % 2, [5, 3, 0, 2, 4, 6, 1][k % 7], k % 3
+        a = gpu_compress(sc, w, h, img, fmt, dither, metric, -1, refine)
+        b = oracle.compress(sc, w, h, img, fmt, dither, metric, -1, refine)
+        assert np.array_equal(a, b), (w, h, sc, hex(fmt), dither, metric, refine)
+
+
+def test_strip_device_sources(lib, oracle):
+    """The device API on the fused kernel: a 16-byte aligned RGBA source (tensor
+    copies), the same pixels 4 bytes further on (vector loads), an image under
+    256 texels, and block rows written `dst_pitch` apart."""
+    torch = pytest.importorskip("torch")
+    for w, h, fmt in ((1000, 333, 0x83F1), (96, 2, 0x83F3), (2051, 19, 0x83F2)):
+        img = workloads.plain_rgba(21, w, h).reshape(-1)
+        want = oracle.compress(4, w, h, img, fmt, 1, s2.WAVG, -1, 1)
+        n, row = s2.compressed_size(w, h, fmt), ((w + 3) // 4) * s2.block_bytes(fmt)
+        for shift in (0, 4):
+            buf = torch.zeros(img.size + 64, dtype=torch.uint8, device="cuda")
+            buf[shift:shift + img.size] = torch.from_numpy(img.copy()).cuda()
+            d_dst = torch.full((n + 64 * ((h + 3) // 4),), 0x5A, dtype=torch.uint8, device="cuda")
+            pitch = row + 64
+            s2.gpu_compress(4, w, h, buf.data_ptr() + shift, fmt, d_dst, dst_pitch=pitch,
+                            opt=s2.options(1, s2.WAVG, -1, 1))
+            s2.gpu_synchronize()
+            got = d_dst.cpu().numpy().reshape(-1, pitch)[:, :row].reshape(-1)[:n]
+            assert np.array_equal(got, want), (w, h, hex(fmt), shift)
+
+
+def test_strip_pipelined_host_path(lib, oracle):
+    """tx_compress_dxtn on images of at least 4 Mi texels in quick mode: the
+    image goes up in ranges of bands and each range is one fused launch whose
+    look-back reaches into the ranges before it."""
+    for w, h, fmt, sc, dither in ((2048, 2051, 0x83F1, 4, 1), (8192, 515, 0x83F3, 4, 1), (3001, 1500, 0x83F2, 3, 0)):
+        img = workloads.plain_rgba(22, w, h)[:, :, :sc].reshape(-1) if sc == 4 else \
+            np.ascontiguousarray(workloads.plain_rgba(22, w, h)[:, :, :3]).reshape(-1)
+        a = gpu_compress(sc, w, h, img, fmt, dither, s2.WAVG, -1, 1)
+        b = oracle.compress(sc, w, h, img, fmt, dither, s2.WAVG, -1, 1)
+        assert np.array_equal(a, b), (w, h, hex(fmt), sc, dither)
