@@ -579,6 +579,31 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
     value = args.steps * texels / t_batch
     single = args.steps * texels / t_single
 
+    # where the time goes, by level size: each class of images as a batch of
+    # its own and through the per-image path (same rand words)
+    breakdown = {}
+    for cls, lo, hi in (("le_64x64", 0, 64 * 64), ("le_256x256", 64 * 64, 256 * 256), ("gt_256x256", 256 * 256, 1 << 62)):
+        sub = [im for im in images if lo < im["width"] * im["height"] <= hi]
+        if not sub:
+            continue
+        tex = sum(im["width"] * im["height"] for im in sub)
+        sub_out = [torch.empty_like(im["dst"]) for im in sub]
+        sub_arr = s2.image_array([dict(im, dst=d) for im, d in zip(sub, sub_out)])
+        sb = s2.Batch(sub, opt)
+        sb.run(sp)
+        s2.gpu_compress_each(sub, opt, sp, arr=sub_arr)
+        s2.gpu_synchronize(sp)
+        tb = timed(lambda: sb.run(sp))
+        te = timed(lambda: s2.gpu_compress_each(sub, opt, sp, arr=sub_arr))
+        s2.gpu_synchronize(sp)
+        sb.close()
+        breakdown[cls] = {"images": len(sub), "texels": tex, "batched_ms": 1000 * tb / args.steps,
+                          "per_image_ms": 1000 * te / args.steps, "per_image_over_batched": te / tb,
+                          "share_of_per_image_time": None}
+    tot_e = sum(b["per_image_ms"] for b in breakdown.values())
+    for b in breakdown.values():
+        b["share_of_per_image_time"] = b["per_image_ms"] / tot_e if tot_e else None
+
     # end to end through the batch API as a reference user calls it: pinned
     # host pixels in, blocks out, and the random candidates drawn from the
     # process's libc rand() stream (in image order, as one tx_compress_dxtn
@@ -672,7 +697,8 @@ def run_batch_workload(args, wl_name: str, wl: dict) -> None:
                            launch_layout=layouts or "default"),
             "per_image": {"value": single, "unit": "texels/s", "ms_per_step": 1000 * t_single / args.steps,
                           "launches_per_step": None},
-            "batched_over_per_image": value / single, "bit_exact_batched_vs_per_image": bit_exact,
+            "batched_over_per_image": value / single, "by_level_size": breakdown,
+            "bit_exact_batched_vs_per_image": bit_exact,
             **oracle_check,
             "per_image_tx_compress_dxtn": {"value": texels / t_host, "unit": "texels/s", "ms_per_step": 1000 * t_host,
                                            "note": "one synchronous call per image, pinned host buffers"},

@@ -836,12 +836,17 @@ struct Batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t done = nullptr;
   int kernels = 0;                      // kernels per run
-  // prepared launch descriptors (device tables already uploaded)
-  DitherWork dwork{};
-  std::vector<DitherArgs> fs_items;     // Floyd-Steinberg: one launch per image
+  // prepared launch descriptors (device tables already uploaded), per group
+  // of consecutive images (see kBatchGroupTexels)
+  struct Group {
+    DitherWork dwork{};
+    int fs_first = 0, fs_count = 0;  // Floyd-Steinberg: one launch per image
+    EncodeWork ework[3]{};
+    bool has_fmt[3] = {false, false, false};
+  };
+  std::vector<Group> groups;
+  std::vector<DitherArgs> fs_items;
   std::vector<size_t> fs_off;
-  EncodeWork ework[3]{};
-  bool has_fmt[3] = {false, false, false};
 
   ~Batch() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -855,23 +860,51 @@ struct Batch {
 };
 
 
+// A batch runs as groups of consecutive images of at most this many texels
+// (the last may exceed it by one image): a group's dither writes its texel
+// words (4 bytes each, 16 MB here) and its encoder launches read them back
+// while they are still in the 129 MB L2.  One dither launch over a whole
+// batch of 64 normal maps of 2048^2 (1.07 GB of texel words) left the
+// encoder 3% slower than one launch pair per image.  A group of one image
+// passes its records by value, as a single-image launch does, instead of
+// through the device tables.
+constexpr long long kBatchGroupTexels = 4ll << 20;
+
 // Lay out, allocate and upload everything a batch's launches need.
 int batch_prepare(Batch& b, Context& c) {
   const int n = int(b.items.size());
   const long long tile_tex = dither_tile_texels();
-  // tables laid out in b.tables: DitherItem[n], tile offsets[n], then per
-  // format EncodeArgs[n_f] and block offsets[n_f]
+  // groups of consecutive images
+  std::vector<int> group_of(n);
+  std::vector<int> first_of_group;
+  {
+    long long tex = 0;
+    for (int i = 0; i < n; ++i) {
+      const long long npx = (long long)b.items[i].width * b.items[i].height;
+      if (i == 0 || tex >= kBatchGroupTexels) {
+        first_of_group.push_back(i);
+        tex = 0;
+      }
+      group_of[i] = int(first_of_group.size()) - 1;
+      tex += npx;
+    }
+  }
+  const int ng = int(first_of_group.size());
+  // tables laid out in b.tables: DitherItem[n], tile offsets[n] (from each
+  // group's first tile), then per format EncodeArgs[n_f] and block offsets
+  // (from each group's first block of that format)
   std::vector<DitherItem> ditems(n);
   std::vector<long long> toff(n);
   std::vector<long long> tex_off(n);
-  long long tiles = 0, texels = 0;
+  std::vector<long long> group_tiles(ng, 0);
+  long long texels = 0;
   for (int i = 0; i < n; ++i) {
     const s2tc_image& im = b.items[i];
     const long long npx = (long long)im.width * im.height;
     tex_off[i] = texels;
     texels += (npx + 3) & ~3ll;  // 16-byte aligned texel rows of each image
-    toff[i] = tiles;
-    tiles += (npx + tile_tex - 1) / tile_tex;
+    toff[i] = group_tiles[group_of[i]];
+    group_tiles[group_of[i]] += (npx + tile_tex - 1) / tile_tex;
   }
   if (!b.t565.reserve(size_t(texels) * 4 + 64, "cudaMalloc(batch texels)")) return ST_OUT_OF_MEMORY;
   for (int i = 0; i < n; ++i) {
@@ -880,16 +913,23 @@ int batch_prepare(Batch& b, Context& c) {
     ditems[i] = DitherItem{static_cast<const uint8_t*>(im.src), im.width, im.height, im.srccomps == 3 ? 3 : 4,
                            alpha_bits(dxt), b.t565.as<uint32_t>() + tex_off[i]};
   }
-  // per-format encode tables
+  // per-format encode tables, in image order; per group and format the first
+  // entry and the count
   std::vector<EncodeArgs> eargs[3];
   std::vector<long long> eoff[3];
-  long long etotal[3] = {0, 0, 0};
+  std::vector<int> gfirst[3], gcount[3];
+  std::vector<long long> gblocks[3];
+  for (int d = 0; d < 3; ++d) {
+    gfirst[d].assign(ng, 0);
+    gcount[d].assign(ng, 0);
+    gblocks[d].assign(ng, 0);
+  }
   const int per_block_words[3] = {b.opt.nrandom > 0 ? b.opt.nrandom * 3 : 0, b.opt.nrandom > 0 ? b.opt.nrandom * 3 : 0,
                                   b.opt.nrandom > 0 ? b.opt.nrandom * 4 : 0};
   long long rand_pos = 0;
   for (int i = 0; i < n; ++i) {
     const s2tc_image& im = b.items[i];
-    const int dxt = format_dxt(im.format);
+    const int dxt = format_dxt(im.format), g = group_of[i];
     EncodeArgs ea{};
     ea.t565 = b.t565.as<uint32_t>() + tex_off[i];
     ea.width = im.width;
@@ -914,8 +954,10 @@ int batch_prepare(Batch& b, Context& c) {
         rand_pos += (long long)ea.bw * ea.bh * per_block_words[dxt];
       }
     }
-    eoff[dxt].push_back(etotal[dxt]);
-    etotal[dxt] += (long long)ea.bw * ea.bh;
+    if (gcount[dxt][g] == 0) gfirst[dxt][g] = int(eargs[dxt].size());
+    gcount[dxt][g]++;
+    eoff[dxt].push_back(gblocks[dxt][g]);
+    gblocks[dxt][g] += (long long)ea.bw * ea.bh;
     eargs[dxt].push_back(ea);
   }
   // upload the tables (pinned staging, copied inside the graph)
@@ -944,9 +986,12 @@ int batch_prepare(Batch& b, Context& c) {
     return ST_CUDA_ERROR;
   unsigned char* tb = b.tables.as<unsigned char>();
 
-  // scratch: SIMPLE/NONE tiles, or one Floyd-Steinberg area per image
+  // scratch: SIMPLE/NONE tiles of the largest group (groups run in stream
+  // order and share it), or one Floyd-Steinberg area per image
   std::vector<size_t> fs_off(n, 0);
-  size_t scratch = dither_batch_scratch_bytes(tiles);
+  long long max_tiles = 0;
+  for (long long t : group_tiles) max_tiles = std::max(max_tiles, t);
+  size_t scratch = dither_batch_scratch_bytes(max_tiles);
   if (b.opt.dither == DI_FLOYDSTEINBERG) {
     scratch = 0;
     for (int i = 0; i < n; ++i) {
@@ -971,24 +1016,40 @@ int batch_prepare(Batch& b, Context& c) {
       da.error = c.err.as<int>();
       b.fs_items.push_back(da);
     }
-  } else {
-    b.dwork = DitherWork{};
-    b.dwork.items = reinterpret_cast<const DitherItem*>(tb + o_ditems);
-    b.dwork.tile_offsets = reinterpret_cast<const long long*>(tb + o_toff);
-    b.dwork.nitems = n;
-    b.dwork.total_tiles = tiles;
-    b.dwork.error = c.err.as<int>();
   }
-  for (int d = 0; d < 3; ++d) {
-    b.has_fmt[d] = !eargs[d].empty();
-    if (!b.has_fmt[d]) continue;
-    EncodeWork& w = b.ework[d];
-    w = EncodeWork{};
-    w.items = reinterpret_cast<const EncodeArgs*>(tb + o_eargs[d]);
-    w.offsets = reinterpret_cast<const long long*>(tb + o_eoff[d]);
-    w.nitems = int(eargs[d].size());
-    w.total = etotal[d];
-    w.nrandom = b.opt.nrandom;
+  b.groups.assign(ng, Batch::Group{});
+  for (int g = 0; g < ng; ++g) {
+    Batch::Group& G = b.groups[g];
+    const int i0 = first_of_group[g], i1 = g + 1 < ng ? first_of_group[g + 1] : n;
+    G.fs_first = i0;
+    G.fs_count = i1 - i0;
+    if (b.opt.dither != DI_FLOYDSTEINBERG) {
+      G.dwork = DitherWork{};
+      if (i1 - i0 == 1) {
+        G.dwork.single = ditems[i0];
+      } else {
+        G.dwork.items = reinterpret_cast<const DitherItem*>(tb + o_ditems) + i0;
+        G.dwork.tile_offsets = reinterpret_cast<const long long*>(tb + o_toff) + i0;
+      }
+      G.dwork.nitems = i1 - i0;
+      G.dwork.total_tiles = group_tiles[g];
+      G.dwork.error = c.err.as<int>();
+    }
+    for (int d = 0; d < 3; ++d) {
+      G.has_fmt[d] = gcount[d][g] > 0;
+      if (!G.has_fmt[d]) continue;
+      EncodeWork& w = G.ework[d];
+      w = EncodeWork{};
+      if (gcount[d][g] == 1) {
+        w.single = eargs[d][gfirst[d][g]];
+      } else {
+        w.items = reinterpret_cast<const EncodeArgs*>(tb + o_eargs[d]) + gfirst[d][g];
+        w.offsets = reinterpret_cast<const long long*>(tb + o_eoff[d]) + gfirst[d][g];
+      }
+      w.nitems = gcount[d][g];
+      w.total = gblocks[d][g];
+      w.nrandom = b.opt.nrandom;
+    }
   }
   return ST_OK;
 }
@@ -1007,19 +1068,21 @@ int batch_launch(Batch& b, cudaStream_t s) {
                  "batch rand upload"))
       return ST_CUDA_ERROR;
   }
-  if (b.opt.dither == DI_FLOYDSTEINBERG) {
-    for (size_t i = 0; i < b.fs_items.size(); ++i)
-      if (!cuda_ok(launch_dither(b.fs_items[i], DI_FLOYDSTEINBERG, b.scratch.as<uint8_t>() + b.fs_off[i], s),
-                   "batch dither"))
+  for (const Batch::Group& G : b.groups) {
+    if (b.opt.dither == DI_FLOYDSTEINBERG) {
+      for (int i = G.fs_first; i < G.fs_first + G.fs_count; ++i)
+        if (!cuda_ok(launch_dither(b.fs_items[i], DI_FLOYDSTEINBERG, b.scratch.as<uint8_t>() + b.fs_off[i], s),
+                     "batch dither"))
+          return ST_CUDA_ERROR;
+    } else {
+      if (!cuda_ok(launch_dither_batch(G.dwork, b.opt.dither, b.scratch.as<uint8_t>(), s), "batch dither"))
         return ST_CUDA_ERROR;
-  } else {
-    if (!cuda_ok(launch_dither_batch(b.dwork, b.opt.dither, b.scratch.as<uint8_t>(), s), "batch dither"))
-      return ST_CUDA_ERROR;
-  }
-  for (int d = 0; d < 3; ++d) {
-    if (!b.has_fmt[d]) continue;
-    if (!cuda_ok(launch_encode(b.ework[d], d, b.opt.metric, b.normal, b.opt.refine, s), "batch encode"))
-      return ST_CUDA_ERROR;
+    }
+    for (int d = 0; d < 3; ++d) {
+      if (!G.has_fmt[d]) continue;
+      if (!cuda_ok(launch_encode(G.ework[d], d, b.opt.metric, b.normal, b.opt.refine, s), "batch encode"))
+        return ST_CUDA_ERROR;
+    }
   }
   b.kernels = int(launches_so_far() - l0);
   return ST_OK;

@@ -931,8 +931,12 @@ __device__ __forceinline__ int dedup(int mm, int lane, int nslots, Slot slot, ui
   return nu;
 }
 
+// CTAs per SM the register budget allows: at 64 random candidates a CTA of
+// four warps holds about 40 KB of shared memory with 16-bit distance rows
+// (five fit an SM) and 53 KB with 32-bit rows (four fit), so the 32-bit
+// metrics get the registers of four CTAs per SM.
 #ifndef S2TC_RAND_MINBLOCKS
-#define S2TC_RAND_MINBLOCKS 5
+#define S2TC_RAND_MINBLOCKS (kSmallDist ? 5 : 4)
 #endif
 template <int DXT, int REFINE>
 __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode_rand(EncodeWork w, int m) {
