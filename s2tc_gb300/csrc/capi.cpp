@@ -120,6 +120,7 @@ struct Context {
   DevBuf small_dev;      // small quick-mode calls: pixels, scan state, flag, blocks
   PinnedBuf small_host;  // ... and their pinned mirror
   PinnedBuf host_flag;  // where the timeout flag is read back to
+  int pageable_access = 0;  // the device reads and writes pageable host memory coherently
 
   bool init() {
     if (ready) return true;
@@ -136,6 +137,12 @@ struct Context {
     if (!cuda_ok(cudaMemset(err.p, 0, sizeof(int) * 4), "cudaMemset")) return false;
     // err[2]: the carried alpha endpoint of tx_compress_dxtn calls (-1: none yet)
     if (!cuda_ok(cudaMemset(err.as<int>() + 2, 0xFF, sizeof(int)), "cudaMemset")) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable_access, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      cudaGetLastError();
+      pageable_access = 0;
+    }
     ready = true;
     return true;
   }
@@ -679,6 +686,47 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
 // (1024x1024: 348 us against 96 us).
 constexpr long long kSmallCallTexels = 1ll << 16;
 
+// Where the device reads and writes pageable host memory coherently (a Grace
+// host's page tables, cudaDevAttrPageableMemoryAccess), the kernel takes the
+// caller's pixels and writes the caller's blocks itself: the call is one
+// launch and one wait (plus one memset of the scan state when the image has
+// more than one band), with no staging copies.  Overlapping output rows (a
+// dstRowStride below the padded row) keep the staging path, whose host copy
+// writes the rows in order.
+bool compress_host_direct(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
+                          unsigned char* dest, long long diff, const s2tc_options& opt, const StripPlan& plan) {
+  const int bw = (width + 3) / 4, bs = block_bytes(dxt);
+  const size_t row_bytes = size_t(bw) * bs;
+  const size_t o_status = 16, o_aggs = align_up(o_status + size_t(plan.bands) * 8, 16);
+  if (!c.small_dev.reserve(o_aggs + size_t(plan.bands) * 72, "cudaMalloc(small call)") ||
+      !c.small_host.reserve(16, "cudaMallocHost(small call)"))
+    return true;
+  volatile int* flag = static_cast<volatile int*>(c.small_host.p);
+  *flag = 0;
+  uint8_t* d = c.small_dev.as<uint8_t>();
+  StripArgs sa = strip_args(plan, sc, width, height, src, dxt, opt.dither, dest, (long long)row_bytes + diff,
+                            const_cast<int*>(flag));
+  sa.use_tma = 0;
+  sa.scan.ticket = reinterpret_cast<unsigned int*>(d);
+  sa.scan.status = reinterpret_cast<unsigned long long*>(d + o_status);
+  sa.scan.aggs = d + o_aggs;
+  sa.single_band = plan.bands == 1;
+  cudaStream_t s = c.stream;
+  if (!sa.single_band && !cuda_ok(cudaMemsetAsync(d, 0, o_aggs, s), "cudaMemsetAsync")) return true;
+  cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
+  if (tev && (!cuda_ok(cudaEventRecord(tev[0], s), "cudaEventRecord") ||
+              !cuda_ok(cudaEventRecord(tev[1], s), "cudaEventRecord")))
+    return true;
+  if (!cuda_ok(launch_strip(sa, nullptr, dxt, opt.metric, opt.refine, nullptr, s), "strip launch")) return true;
+  if (tev) {
+    if (!cuda_ok(cudaEventRecord(tev[2], s), "cudaEventRecord")) return true;
+    c.timed_calls++;
+  }
+  if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return true;
+  if (*flag) set_error("a bounded wait in the dither scan gave up");
+  return true;
+}
+
 bool compress_host_small(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                          unsigned char* dest, int dstRowStride, const s2tc_options& opt, bool* done) {
   *done = false;
@@ -688,6 +736,12 @@ bool compress_host_small(Context& c, int sc, int width, int height, const unsign
   *done = true;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
   const size_t row_bytes = size_t(bw) * bs, out_bytes = row_bytes * bh;
+  {
+    const long long diff =
+        dstRowStride >= width * (bs / 4) ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs / 4) : 0;
+    if (c.pageable_access == 1 && diff >= 0)
+      return compress_host_direct(c, sc, width, height, src, dxt, dest, diff, opt, plan);
+  }
   const size_t o_ticket = align_up(size_t(npx) * sc, 256), o_status = o_ticket + 16;
   const size_t o_flag = align_up(o_status + size_t(plan.bands) * 8, 16), o_blocks = o_flag + 16;
   const size_t o_aggs = align_up(o_blocks + out_bytes, 16), total = o_aggs + size_t(plan.bands) * 72;

@@ -1357,7 +1357,7 @@ __global__ void __launch_bounds__(kStripThreads, 2) k_strip_quick(const __grid_c
   __shared__ unsigned int s_ticket;
   const int t = threadIdx.x;
   init_tables(sm);
-  if (t == 0) s_ticket = atomicAdd(a.scan.ticket, 1u);
+  if (t == 0) s_ticket = a.single_band ? blockIdx.x : atomicAdd(a.scan.ticket, 1u);
   bulk_init(sm);
   __syncthreads();
   if ((long long)s_ticket >= a.nbands) return;
@@ -1504,7 +1504,8 @@ cudaError_t S2TC_CAT(launch_strip_m, S2TC_METRIC)(StripArgs a, const void* tmap,
     cudaError_t e = cudaMemsetAsync(a.scan.status + a.band_base, 0, a.nbands * sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.scan.ticket, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-  } else if (!a.scan.status || !a.scan.aggs || !a.scan.ticket || a.band_base != 0) {
+  } else if (!a.scan.status || !a.scan.aggs || (!a.scan.ticket && !a.single_band) || a.band_base != 0 ||
+             (a.single_band && a.nbands != 1)) {
     return cudaErrorInvalidValue;
   }
   CUtensorMap map;

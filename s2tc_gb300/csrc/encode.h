@@ -80,6 +80,7 @@ struct StripArgs {
   long long band_base;  // bands [band_base, band_base + nbands) of the image
   long long nbands;
   long long image_bands;  // bands of the whole image (the scan state's layout)
+  int single_band;      // one band in all: the CTA takes band 0 without a ticket
   int use_tma;          // RGBA8 rows through the tensor map (16-byte aligned source)
   long long tma_rows;   // 256-texel rows the tensor map covers (texels / 256)
   DitherWork scan;      // scan state: status, aggs, ticket (zeroed by the launcher), error
