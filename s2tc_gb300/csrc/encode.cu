@@ -621,6 +621,9 @@ __global__ void __launch_bounds__(kThreadsPerCta) k_encode(EncodeWork w) {
 
 constexpr int kRandWarps = 4;
 constexpr unsigned kFull = 0xFFFFFFFFu;
+// Unique candidates up to which a pair search packs (sum, i, j) into 32 bits
+// (positions as a * 90 + b < 8192, 13 bits).
+constexpr int kKeyPositions = 90;
 
 // Colour distance rows fit in 16 bits for the AVG family (at most
 // 4*31^2 + 4*63^2 + 31^2 = 20681); they are then packed two per word.
@@ -854,7 +857,8 @@ constexpr int kPairUnroll = S2TC_PAIR_UNROLL;  // partner rows unrolled per tile
 // Walks every pair i < j < mm: 8-row tiles (I, J), I <= J, four groups of
 // eight lanes per warp, each group one tile at a time; lane r of a group owns
 // row I*8 + r and visits the tile's eight partner rows.  `load(k, row)` reads
-// row k, `sum(a, b)` combines two rows, `visit(i, j, s)` sees every pair once.
+// row k, `sum(a, b)` combines two rows, `visit(i, j, s, valid)` sees every
+// pair once with `valid` set (and some clamped non-pairs with it clear).
 template <class RowT, class Load, class Sum, class Visit>
 __device__ __forceinline__ void tiled_pairs(int mm, int lane, Load load, Sum sum, Visit visit) {
   const int g = lane >> 3, r = lane & 7;
@@ -878,7 +882,7 @@ __device__ __forceinline__ void tiled_pairs(int mm, int lane, Load load, Sum sum
       RowT rj;
       load(min(j, mm - 1), rj);
       const auto v = sum(ri, rj);
-      if (ok && j < mm && j > i) visit(i, j, v);
+      visit(i, j, v, ok && j < mm && j > i);
     }
   }
 }
@@ -1062,7 +1066,11 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
     {
       uint64_t best = ~0ull;
       bool neg = false;
-      if (kSmallDist) {
+      if (kSmallDist && nuc <= kKeyPositions) {
+        // 32-bit keys (sum << 13 | a * 90 + b): the sums of 16-bit rows stay
+        // below 2^19, and the unique list is in ascending candidate order, so
+        // its positions order pairs as the candidates' indices do
+        uint32_t best32 = 0xFFFFFFFFu;
         tiled_pairs<RowU16>(
             nuc, lane,
             [&](int k, RowU16& rw) {
@@ -1071,8 +1079,26 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
               rw.q[1] = q[1];
             },
             [](const RowU16& x, const RowU16& y) { return pair_sum16(x.q, y.q); },
-            [&](int a, int b, uint32_t v) {
-              if (v > uint32_t(best >> 32)) return;  // cannot win; skip the index lookups
+            [&](int a, int b, uint32_t v, bool valid) {
+              const uint32_t key = (v << 13) | uint32_t(a * kKeyPositions + b);
+              best32 = min(best32, valid ? key : 0xFFFFFFFFu);
+            });
+        best32 = __reduce_min_sync(kFull, best32);
+        if (best32 != 0xFFFFFFFFu) {  // none when every candidate has one value
+          const int pa = int((best32 & 8191u) / kKeyPositions), pb = int((best32 & 8191u) % kKeyPositions);
+          best = (uint64_t(best32 >> 13) << 32) | (uint32_t(ncs ? sUc[pa] : pa) << 16) | uint32_t(ncs ? sUc[pb] : pb);
+        }
+      } else if (kSmallDist) {
+        tiled_pairs<RowU16>(
+            nuc, lane,
+            [&](int k, RowU16& rw) {
+              const uint4* q = reinterpret_cast<const uint4*>(sD + size_t(k) * kRowBytes);
+              rw.q[0] = q[0];
+              rw.q[1] = q[1];
+            },
+            [](const RowU16& x, const RowU16& y) { return pair_sum16(x.q, y.q); },
+            [&](int a, int b, uint32_t v, bool valid) {
+              if (!valid || v > uint32_t(best >> 32)) return;  // cannot win; skip the index lookups
               const uint32_t ia = ncs ? sUc[a] : a, ib = ncs ? sUc[b] : b;
               const uint64_t key = (uint64_t(v) << 32) | (ia << 16) | ib;
               best = key < best ? key : best;
@@ -1086,7 +1112,8 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
               for (int t = 0; t < 4; ++t) rw.q[t] = q[t];
             },
             [](const RowI32& x, const RowI32& y) { return pair_sum(x.q, y.q); },
-            [&](int a, int b, int32_t v) {
+            [&](int a, int b, int32_t v, bool valid) {
+              if (!valid) return;
               neg |= v < 0;
               if (v < 0 || uint32_t(v) > uint32_t(best >> 32)) return;
               const uint32_t ia = ncs ? sUc[a] : a, ib = ncs ? sUc[b] : b;
@@ -1172,19 +1199,42 @@ __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode
       }
       __syncwarp();
       uint64_t best = ~0ull;
-      tiled_pairs<RowU16>(
-          nua, lane,
-          [&](int k, RowU16& rw) {
-            const uint4* q = reinterpret_cast<const uint4*>(sE + size_t(k) * 32);
-            rw.q[0] = q[0];
-            rw.q[1] = q[1];
-          },
-          [](const RowU16& x, const RowU16& y) { return pair_sq_sum16(x.q, y.q); },
-          [&](int a, int b, uint32_t v) {
-            if (v > uint32_t(best >> 32)) return;
-            const uint64_t key = (uint64_t(v) << 32) | (uint32_t(sUa[a]) << 16) | uint32_t(sUa[b]);
-            best = key < best ? key : best;
-          });
+      if (nua <= kKeyPositions) {
+        // 32-bit keys: a capped alpha distance is at most 127, so the sums stay
+        // below 16 * 127^2 < 2^18 (see the colour search)
+        uint32_t best32 = 0xFFFFFFFFu;
+        tiled_pairs<RowU16>(
+            nua, lane,
+            [&](int k, RowU16& rw) {
+              const uint4* q = reinterpret_cast<const uint4*>(sE + size_t(k) * 32);
+              rw.q[0] = q[0];
+              rw.q[1] = q[1];
+            },
+            [](const RowU16& x, const RowU16& y) { return pair_sq_sum16(x.q, y.q); },
+            [&](int a, int b, uint32_t v, bool valid) {
+              const uint32_t key = (v << 13) | uint32_t(a * kKeyPositions + b);
+              best32 = min(best32, valid ? key : 0xFFFFFFFFu);
+            });
+        best32 = __reduce_min_sync(kFull, best32);
+        if (best32 != 0xFFFFFFFFu) {
+          const int pa = int((best32 & 8191u) / kKeyPositions), pb = int((best32 & 8191u) % kKeyPositions);
+          best = (uint64_t(best32 >> 13) << 32) | (uint32_t(sUa[pa]) << 16) | uint32_t(sUa[pb]);
+        }
+      } else {
+        tiled_pairs<RowU16>(
+            nua, lane,
+            [&](int k, RowU16& rw) {
+              const uint4* q = reinterpret_cast<const uint4*>(sE + size_t(k) * 32);
+              rw.q[0] = q[0];
+              rw.q[1] = q[1];
+            },
+            [](const RowU16& x, const RowU16& y) { return pair_sq_sum16(x.q, y.q); },
+            [&](int a, int b, uint32_t v, bool valid) {
+              if (!valid || v > uint32_t(best >> 32)) return;
+              const uint64_t key = (uint64_t(v) << 32) | (uint32_t(sUa[a]) << 16) | uint32_t(sUa[b]);
+              best = key < best ? key : best;
+            });
+      }
       for (int ua = lane; ua < nua; ua += 32) {
         const int x = sUa[ua];
         const uint32_t y = sTab[kDedupSlots + sA[x]];
