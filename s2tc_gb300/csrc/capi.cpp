@@ -143,6 +143,7 @@ struct Context {
       cudaGetLastError();
       pageable_access = 0;
     }
+    if (!cuda_ok(nm_table_init(stream), "NORMALMAP table")) return false;
     ready = true;
     return true;
   }

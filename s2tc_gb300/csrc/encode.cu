@@ -1533,10 +1533,32 @@ cudaError_t launch_strip_d(const StripArgs& a, const CUtensorMap& map, int refin
   }
 }
 
+#if S2TC_METRIC == 7
+__global__ void k_nm_table() {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < (1 << 16)) {
+    const NUnit v = nm_unit(C3{(k >> 11) & 31, (k >> 5) & 63, k & 31});
+    g_nm_table[k] = make_float4(v.x, v.y, v.z, 0.0f);
+  }
+}
+__global__ void k_nm_ready() { g_nm_ready = 1; }
+#endif
+
 }  // namespace
 
 #define S2TC_CAT2(a, b) a##b
 #define S2TC_CAT(a, b) S2TC_CAT2(a, b)
+
+#if S2TC_METRIC == 7
+cudaError_t nm_table_init(cudaStream_t s) {
+  count_launches(2);
+  k_nm_table<<<256, 256, 0, s>>>();
+  k_nm_ready<<<1, 1, 0, s>>>();
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+#endif
 
 cudaError_t S2TC_CAT(launch_strip_m, S2TC_METRIC)(StripArgs a, const void* tmap, int dxt, int refine,
                                                   uint8_t* scratch, cudaStream_t s) {

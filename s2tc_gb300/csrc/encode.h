@@ -116,6 +116,11 @@ inline cudaError_t launch_strip(const StripArgs& a, const void* tmap, int dxt, i
   }
 }
 
+// Builds NORMALMAP's table of prepared colours on the current device and
+// waits for it (once per device, outside any stream capture; kernels compute
+// the form themselves until the table is ready, so calling it is optional).
+cudaError_t nm_table_init(cudaStream_t s);
+
 // Launch layout of the encoder kernels for one mode (the autotuner's knobs;
 // no effect on the bytes).
 enum { kLayoutQuick = 0, kLayoutFull = 1, kLayoutRand = 2 };

@@ -80,6 +80,25 @@ __device__ __forceinline__ int32_t nm_dist(NUnit a, NUnit b) {
   return __float2int_rz(__fmul_rn(100000.0f, s));
 }
 
+// NORMALMAP's prepared form of every 5:6:5 colour, computed once per device by
+// nm_unit itself (encode.cu, nm_table_init) into a 1 MB table in the
+// translation unit of that metric; until the table is ready (flag set after
+// the table kernel has completed) the form is computed on the spot.  Either
+// way the bits are nm_unit's.
+#if defined(S2TC_METRIC) && S2TC_METRIC == 7
+static __device__ float4 g_nm_table[1 << 16];
+static __device__ int g_nm_ready;
+__device__ __forceinline__ NUnit nm_prepared(C3 c) {
+  if (g_nm_ready) {
+    const float4 v = __ldg(&g_nm_table[(c.r << 11) | (c.g << 5) | c.b]);
+    return NUnit{v.x, v.y, v.z};
+  }
+  return nm_unit(c);
+}
+#else
+__device__ __forceinline__ NUnit nm_prepared(C3 c) { return nm_unit(c); }
+#endif
+
 // Each metric is evaluated on a per-colour "prepared" form computed once per
 // colour: the squared components for SRGB, (Y, U, V) with the square-rooted
 // luma for SRGB_MIXED, the unit vector for NORMALMAP, the plain components
@@ -130,7 +149,7 @@ __device__ __forceinline__ typename PrepT<METRIC>::T prep(C3 c) {
     const int y = srgb_luma(c.r, c.g, c.b);
     return C3{y, c.r * 191 - y, c.b * 191 - y};
   } else if constexpr (METRIC == CD_NORMALMAP) {
-    return nm_unit(c);
+    return nm_prepared(c);
   } else if constexpr (METRIC == CD_AVG) {  // 4 dr^2 + dg^2 + 4 db^2
     return Pk{uint32_t(2 * c.r) | (uint32_t(c.g) << 8) | (uint32_t(2 * c.b) << 16)};
   } else if constexpr (METRIC == CD_WAVG) {  // 4 dr^2 + 4 dg^2 + db^2
