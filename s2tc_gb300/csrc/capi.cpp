@@ -95,19 +95,22 @@ struct Context {
   DevBuf mips, blocks;  // s2tc_compress_dds: every level's pixels and blocks
   DevBuf rnd_win;       // the rand() stream position for the device generator
   // pipelined tx_compress_dxtn: upload and download streams, per-range events
-  cudaStream_t copy_in = nullptr, copy_out = nullptr, encode_stream[2] = {nullptr, nullptr};
+  // chunks of block rows take the encode streams in turn, so that one
+  // chunk's encode fills the last, partial wave of the ones before it
+  static constexpr int kEncodeStreams = 4;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, encode_stream[kEncodeStreams] = {};
   cudaEvent_t pipe_first = nullptr;  // the first range's encode (it reads the carried endpoint)
-  static constexpr int kPipeRanges = 64;
+  static constexpr int kPipeRanges = 128;
   cudaEvent_t pipe_in[kPipeRanges] = {}, pipe_mid[kPipeRanges] = {}, pipe_out[kPipeRanges] = {};
   bool pipe_ready = false;
   bool init_pipe() {
     if (pipe_ready) return true;
     if (!cuda_ok(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !cuda_ok(cudaStreamCreateWithFlags(&encode_stream[0], cudaStreamNonBlocking), "cudaStreamCreate") ||
-        !cuda_ok(cudaStreamCreateWithFlags(&encode_stream[1], cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaEventCreateWithFlags(&pipe_first, cudaEventDisableTiming), "cudaEventCreate"))
       return false;
+    for (cudaStream_t& e : encode_stream)
+      if (!cuda_ok(cudaStreamCreateWithFlags(&e, cudaStreamNonBlocking), "cudaStreamCreate")) return false;
     for (int i = 0; i < kPipeRanges; ++i)
       if (!cuda_ok(cudaEventCreateWithFlags(&pipe_in[i], cudaEventDisableTiming), "cudaEventCreate") ||
           !cuda_ok(cudaEventCreateWithFlags(&pipe_mid[i], cudaEventDisableTiming), "cudaEventCreate") ||
@@ -462,30 +465,65 @@ bool host_pinned(const void* p) {
 }
 
 // tx_compress_dxtn on a large image, pipelined: the image goes up in ranges of
-// whole dither tiles on one copy stream; the dither stream scans each range
-// as it lands (the scan's look-back reaches into the ranges before it); two
+// whole dither tiles on one copy stream; the compute stream scans each range
+// as it lands (the scan's look-back reaches into the ranges before it); the
 // encode streams, in turn, encode the block rows whose four texel rows are
 // complete while the next range is dithered; a second copy stream brings those rows
-// back (per range when `dest` is pinned, else at the end).  Same kernels and
+// back (per chunk when `dest` is pinned, else at the end).  Same kernels and
 // bytes as the unpipelined path.  Returns false when the image does not
 // qualify (the caller then takes that path).
-// Ranges: about kPipeTargetRanges of them, at least kPipeRangeTiles tiles
-// each.  Every range costs a dozen stream operations on the host (about 40 µs
-// on the GB300 host), so more ranges starve the GPU; fewer leave more of the
-// first upload and the last encode outside the overlap.  At 4096^2 DXT5
-// all-16 LOOP (0.72 ms of kernels) a call took 0.869 ms in 8 ranges, 0.842 ms
-// in 12 and 0.99 ms in 16.
+// Dither ranges: a dither launch ends 45 to 75 us after the last byte of its
+// range lands, whatever its size (a tile's latency plus the wait for SM slots
+// behind the queued encoder CTAs), and the launches run one after another on
+// one stream.  The host's stream operations are cheap by comparison (about
+// 10 us a range).  So the ranges double in size from kPipeFirstTiles: the
+// first is dithered a few microseconds into the call and the chain of
+// launches stays ahead of the upload.  The encoder takes the finished block
+// rows in chunks of at most 1/kPipeEncodeChunks of the image, each with its own
+// download, so that little is left to do after the last dither range.  At
+// 4096^2 DXT5 all-16 LOOP (0.67 ms of kernels) a call took 0.84 ms in 12
+// equal ranges on two encode streams, 0.81 ms in the doubling ranges with 16
+// chunks on four (one stream: 1.02 ms, two: 0.85 ms).
 constexpr long long kPipeMinTexels = 1ll << 22;
+constexpr long long kPipeFirstTiles = 16;
+constexpr long long kPipeMaxRangeTiles = 512;
+constexpr int kPipeEncodeChunks = 16;
+
+// Tile ends of the dither ranges of a `tiles`-tile image: 16, 32, 64, ...
+// tiles, each at most max(kPipeMaxRangeTiles, tiles / 48) (so at most about
+// 60 ranges); a remainder below kPipeFirstTiles joins the range before it.
+// Returns their number, or 0 past `max_ranges`.
+int dither_ranges(long long tiles, long long* ends, int max_ranges) {
+  const long long cap = std::max(kPipeMaxRangeTiles, (tiles + 47) / 48);
+  long long t = 0, step = kPipeFirstTiles;
+  int n = 0;
+  while (t < tiles) {
+    if (n == max_ranges) return 0;
+    t = std::min(tiles, t + std::min(step, cap));
+    if (tiles - t < kPipeFirstTiles) t = tiles;
+    ends[n++] = t;
+    step *= 2;
+  }
+  return n;
+}
+
+// The strip pipeline's ranges hold at least kPipeRangeTiles dither tiles'
+// worth of texels and are at most kPipeTargetRanges.
 constexpr long long kPipeRangeTiles = 64;
 constexpr long long kPipeTargetRanges = 12;
-// ranges = ceil(tiles / per_range) <= kPipeTargetRanges, as per_range >= ceil(tiles / kPipeTargetRanges)
 static_assert(kPipeTargetRanges <= Context::kPipeRanges, "one event set per range");
 
 // The same for the fused strip kernel (quick mode): the image goes up in
 // ranges of bands on the copy stream, one strip launch per range on the
 // compute stream (its look-back reaches into the ranges before it), and each
 // range's block rows come back on the second copy stream when `dest` is
-// pinned.
+// pinned.  The launches run one after another, and each takes at least the
+// latency of one band (50 to 80 us for 4096-texel rows), so a range carries
+// about kStripRangeBytes of pixels: its upload (about 85 us at the measured
+// 190 GB/s of the host link) then hides the launch before it.  4096^2 DXT1
+// quick: 0.62 ms per call in 12 ranges, 0.59 in 11 ranges of 6 MB, 0.465 in 7
+// of 10 MB, 0.447 in 4 of 16 MB; the bare upload is 0.35 ms.
+constexpr long long kStripRangeBytes = 16ll << 20;
 bool compress_host_pipelined_strip(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                                    unsigned char* dest, long long diff, const s2tc_options& opt,
                                    const StripPlan& plan) {
@@ -495,7 +533,8 @@ bool compress_host_pipelined_strip(Context& c, int sc, int width, int height, co
   const long long row_bytes = (long long)bw * block_bytes(dxt);
   const long long band_texels = 4ll * plan.rows_per_band * width;
   const long long min_bands = std::max(1ll, (kPipeRangeTiles * dither_tile_texels() + band_texels - 1) / band_texels);
-  const long long per_range = std::max(min_bands, (plan.bands + kPipeTargetRanges - 1) / kPipeTargetRanges);
+  const long long target = std::min(kPipeTargetRanges, std::max(1ll, (npx * sc + kStripRangeBytes - 1) / kStripRangeBytes));
+  const long long per_range = std::max(min_bands, (plan.bands + target - 1) / target);
   const int ranges = int((plan.bands + per_range - 1) / per_range);
   if (!c.src.reserve(size_t(npx) * sc + 16, "cudaMalloc(src)")) return true;
   if (!c.dst.reserve(size_t(row_bytes) * bh + 16, "cudaMalloc(dst)")) return true;
@@ -558,15 +597,20 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   const bool normal = normal_mode(opt);
   const int per_block = rand_per_block(opt, dxt);
   if (per_block > 0 && !rand_usable()) return false;
-  if (!c.init_pipe()) return false;
+  const long long tile = dither_tile_texels();
+  const long long tiles = (npx + tile - 1) / tile;
+  long long ends[Context::kPipeRanges];
+  // at most half the events for the dither ranges: encode chunks end at
+  // range ends or at multiples of chunk_rows, so there are fewer than
+  // ranges + kPipeEncodeChunks of them
+  const int ranges = dither_ranges(tiles, ends, Context::kPipeRanges / 2);
+  static_assert(Context::kPipeRanges / 2 + kPipeEncodeChunks < Context::kPipeRanges, "one event per chunk");
+  if (ranges == 0 || !c.init_pipe()) return false;
   *done = true;
   cudaStream_t s = c.stream;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
   const long long row_bytes = (long long)bw * bs;
-  const long long tile = dither_tile_texels();
-  const long long tiles = (npx + tile - 1) / tile;
-  const long long per_range = std::max(kPipeRangeTiles, (tiles + kPipeTargetRanges - 1) / kPipeTargetRanges);
-  const int ranges = int((tiles + per_range - 1) / per_range);
+  const int chunk_rows = std::max(1, (bh + kPipeEncodeChunks - 1) / kPipeEncodeChunks);
   if (!c.src.reserve(size_t(npx) * sc + 16, "cudaMalloc(src)")) return true;
   if (!c.dst.reserve(size_t(row_bytes) * bh + 16, "cudaMalloc(dst)")) return true;
   if (!c.t565.reserve(size_t(npx) * 4 + 16, "cudaMalloc(texels)")) return true;
@@ -618,8 +662,9 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
     ea.leftover_out = c.err.as<int>() + 2;
   }
   int rows_done = 0, nenc = 0;
+  long long t0 = 0;
   for (int r = 0; r < ranges; ++r) {
-    const long long t0 = r * per_range, t1 = std::min(tiles, t0 + per_range);
+    const long long t1 = ends[r];
     const long long p0 = t0 * tile, p1 = std::min(npx, t1 * tile);
     if (!cuda_ok(cudaMemcpyAsync(d_src + p0 * sc, src + p0 * sc, size_t(p1 - p0) * sc, cudaMemcpyHostToDevice,
                                  c.copy_in),
@@ -628,37 +673,38 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
         !cuda_ok(cudaStreamWaitEvent(s, c.pipe_in[r], 0), "cudaStreamWaitEvent") ||
         !cuda_ok(launch_dither_range(da, opt.dither, c.scratch.as<uint8_t>(), t0, t1, s), "dither launch"))
       return true;
+    t0 = t1;
     const int rows_ready = r == ranges - 1 ? bh : int((p1 / width) / 4);
     if (rows_ready <= rows_done) continue;
-    ea.by0 = rows_done;
-    ea.nby = rows_ready - rows_done;
-    ea.rnd = rnd ? rnd + (long long)rows_done * bw * per_block : nullptr;
-    // consecutive ranges alternate between two encode streams, so that one
-    // range's encode fills the last, partial wave of the one before
-    cudaStream_t se = c.encode_stream[nenc & 1];
-    if (!cuda_ok(cudaEventRecord(c.pipe_mid[r], s), "cudaEventRecord") ||
-        !cuda_ok(cudaStreamWaitEvent(se, c.pipe_mid[r], 0), "cudaStreamWaitEvent"))
-      return true;
-    // the last rows write the carried endpoint that the first rows read
-    if (rows_ready == bh && nenc > 0 && (nenc & 1) &&
-        !cuda_ok(cudaStreamWaitEvent(se, c.pipe_first, 0), "cudaStreamWaitEvent"))
-      return true;
-    if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, se), "encode launch")) return true;
-    if (nenc == 0 && !cuda_ok(cudaEventRecord(c.pipe_first, se), "cudaEventRecord")) return true;
-    ++nenc;
-    if (pinned_out) {
-      if (!cuda_ok(cudaEventRecord(c.pipe_out[r], se), "cudaEventRecord") ||
-          !cuda_ok(cudaStreamWaitEvent(c.copy_out, c.pipe_out[r], 0), "cudaStreamWaitEvent") ||
-          !cuda_ok(cudaMemcpy2DAsync(dest + (long long)rows_done * (row_bytes + diff), size_t(row_bytes + diff),
-                                     d_dst + (long long)rows_done * row_bytes, size_t(row_bytes), size_t(row_bytes),
-                                     size_t(rows_ready - rows_done), cudaMemcpyDeviceToHost, c.copy_out),
-                   "output download"))
+    if (!cuda_ok(cudaEventRecord(c.pipe_mid[r], s), "cudaEventRecord")) return true;
+    while (rows_done < rows_ready) {
+      const int rows_end = std::min(rows_ready, (rows_done / chunk_rows + 1) * chunk_rows);
+      ea.by0 = rows_done;
+      ea.nby = rows_end - rows_done;
+      ea.rnd = rnd ? rnd + (long long)rows_done * bw * per_block : nullptr;
+      const int k = nenc % Context::kEncodeStreams;
+      cudaStream_t se = c.encode_stream[k];
+      if (!cuda_ok(cudaStreamWaitEvent(se, c.pipe_mid[r], 0), "cudaStreamWaitEvent")) return true;
+      // the last rows write the carried endpoint that the first rows read
+      if (rows_end == bh && k != 0 &&
+          !cuda_ok(cudaStreamWaitEvent(se, c.pipe_first, 0), "cudaStreamWaitEvent"))
         return true;
+      if (!cuda_ok(launch_encode(ea, dxt, opt.metric, normal, opt.refine, se), "encode launch")) return true;
+      if (nenc == 0 && !cuda_ok(cudaEventRecord(c.pipe_first, se), "cudaEventRecord")) return true;
+      if (pinned_out &&
+          (!cuda_ok(cudaEventRecord(c.pipe_out[nenc], se), "cudaEventRecord") ||
+           !cuda_ok(cudaStreamWaitEvent(c.copy_out, c.pipe_out[nenc], 0), "cudaStreamWaitEvent") ||
+           !cuda_ok(cudaMemcpy2DAsync(dest + (long long)rows_done * (row_bytes + diff), size_t(row_bytes + diff),
+                                      d_dst + (long long)rows_done * row_bytes, size_t(row_bytes), size_t(row_bytes),
+                                      size_t(rows_end - rows_done), cudaMemcpyDeviceToHost, c.copy_out),
+                    "output download")))
+        return true;
+      ++nenc;
+      rows_done = rows_end;
     }
-    rows_done = rows_ready;
   }
   // the compute stream joins the encode streams, then (unpinned output) downloads
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < Context::kEncodeStreams; ++k)
     if (!cuda_ok(cudaEventRecord(c.pipe_mid[k], c.encode_stream[k]), "cudaEventRecord") ||
         !cuda_ok(cudaStreamWaitEvent(s, c.pipe_mid[k], 0), "cudaStreamWaitEvent"))
       return true;

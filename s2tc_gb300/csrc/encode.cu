@@ -1342,6 +1342,10 @@ cudaError_t launch_r(const EncodeWork& a, int refine, cudaStream_t s) {
       case RF_LOOP: k_encode_full16<DXT, RF_LOOP><<<grid16, kThreadsPerCta, 0, s>>>(a); break;
       default: k_encode_full16<DXT, RF_ALWAYS><<<grid16, kThreadsPerCta, 0, s>>>(a); break;
     }
+    // every block of a DXT3/DXT5 image whose sides are multiples of 4 is
+    // whole, and k_encode would leave every one of them
+    if (DXT != DXT1 && !a.items && a.single.width % 4 == 0 && a.single.height % 4 == 0)
+      return cudaGetLastError();
   }
   count_launches(1);
   switch (refine) {

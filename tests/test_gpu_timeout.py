@@ -43,15 +43,20 @@ def test_device_call_reports_timeout_then_recovers(lib, oracle):
     assert np.array_equal(d_dst.cpu().numpy(), want)
 
 
-def test_pipelined_host_call_reports_timeout_then_recovers(lib, oracle):
-    """tx_compress_dxtn on a 2048x2048 image (the pipelined path: the image
-    goes up and is dithered range by range); the held tile sits in the second
-    range, so waits across a range boundary give up too."""
-    w, h, fmt = 2048, 2048, 0x83F1
+@pytest.mark.parametrize("nrandom,w,hold", [(-1, 4096, 300), (0, 2048, 30)])
+def test_pipelined_host_call_reports_timeout_then_recovers(lib, oracle, nrandom, w, hold):
+    """tx_compress_dxtn on the two pipelined paths: the image goes up range by
+    range and each range is scanned as it lands.  The quick mode (nrandom -1,
+    4096x2048) runs the fused strip kernel over 512 bands of one block row in
+    two ranges of 256; the all-texel search (nrandom 0, 2048x2048) runs the
+    dither over 253 tiles of 16640 texels in ranges of 16, 32, 64 and 141.
+    The held band or tile sits in the second range, so waits across a range
+    boundary give up too."""
+    h, fmt = 2048, 0x83F1
     img = workloads.plain_rgba(10, w, h).reshape(-1)
-    s2.set_env(1, s2.WAVG, -1, 1)
+    s2.set_env(1, s2.WAVG, nrandom, 1)
     try:
-        s2.hold_dither_tile(70, 1024)
+        s2.hold_dither_tile(hold, 1024)
         s2.tx_compress_dxtn(4, w, h, img, fmt)
         err = s2.last_error()
     finally:
@@ -59,5 +64,5 @@ def test_pipelined_host_call_reports_timeout_then_recovers(lib, oracle):
     assert "bounded wait" in err
     pyoracle.srand(1)
     got = s2.tx_compress_dxtn(4, w, h, img, fmt)
-    want = oracle.compress(4, w, h, img, fmt, 1, s2.WAVG, -1, 1)
+    want = oracle.compress(4, w, h, img, fmt, 1, s2.WAVG, nrandom, 1)
     assert np.array_equal(got, want)
