@@ -137,19 +137,26 @@ __device__ __forceinline__ void reduce16_rgb(const P* tp, uint32_t mask, Scratch
   int32_t S[120];
 #pragma unroll
   for (int p = 0; p < 120; ++p) S[p] = 0;
+  // two inputs per pass: each sum takes both minima in one three-input add
 #pragma unroll 1
-  for (int k = 0; k < 16; ++k) {
-    if (!((mask >> k) & 1u)) continue;  // a transparent DXT1 texel is no input
-    const P pk = sc.pin[k][t];
-    int32_t col[16];
+  for (int k = 0; k < 16; k += 2) {
+    const P pk = sc.pin[k][t], pk1 = sc.pin[k + 1][t];
+    // a transparent DXT1 texel is no input: its distances count as 0
+    const bool in0 = (mask >> k) & 1u, in1 = (mask >> (k + 1)) & 1u;
+    int32_t col[16], col1[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i)
+    for (int i = 0; i < 16; ++i) {
       col[i] = (kSymmetric || i < k) ? pdist<kMetric>(pin[i], pk) : pdist<kMetric>(pk, pin[i]);
+      col1[i] = (kSymmetric || i < k + 1) ? pdist<kMetric>(pin[i], pk1) : pdist<kMetric>(pk1, pin[i]);
+      col[i] = in0 ? col[i] : 0;
+      col1[i] = in1 ? col1[i] : 0;
+    }
     int p = 0;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
 #pragma unroll
-      for (int j = i + 1; j < 16; ++j, ++p) S[p] = wadd(S[p], min(col[i], col[j]));
+      for (int j = i + 1; j < 16; ++j, ++p)
+        S[p] = int32_t(uint32_t(S[p]) + uint32_t(min(col[i], col[j])) + uint32_t(min(col1[i], col1[j])));
   }
   uint32_t neg = 0;
 #pragma unroll
