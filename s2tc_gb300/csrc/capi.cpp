@@ -14,6 +14,8 @@
 #include <strings.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -739,7 +741,11 @@ constexpr long long kSmallCallTexels = 1ll << 16;
 // launch and one wait (plus one memset of the scan state when the image has
 // more than one band), with no staging copies.  Overlapping output rows (a
 // dstRowStride below the padded row) keep the staging path, whose host copy
-// writes the rows in order.
+// writes the rows in order.  The wait is a poll of a flag in pinned memory
+// that the last band to finish raises after its blocks (bounded: past
+// kSmallPollLimit the stream wait takes over), which returns sooner than the
+// stream wait.
+constexpr auto kSmallPollLimit = std::chrono::milliseconds(5);
 bool compress_host_direct(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                           unsigned char* dest, long long diff, const s2tc_options& opt, const StripPlan& plan) {
   const int bw = (width + 3) / 4, bs = block_bytes(dxt);
@@ -749,7 +755,9 @@ bool compress_host_direct(Context& c, int sc, int width, int height, const unsig
       !c.small_host.reserve(16, "cudaMallocHost(small call)"))
     return true;
   volatile int* flag = static_cast<volatile int*>(c.small_host.p);
+  volatile int* done = flag + 1;
   *flag = 0;
+  *done = 0;
   uint8_t* d = c.small_dev.as<uint8_t>();
   StripArgs sa = strip_args(plan, sc, width, height, src, dxt, opt.dither, dest, (long long)row_bytes + diff,
                             const_cast<int*>(flag));
@@ -758,6 +766,8 @@ bool compress_host_direct(Context& c, int sc, int width, int height, const unsig
   sa.scan.status = reinterpret_cast<unsigned long long*>(d + o_status);
   sa.scan.aggs = d + o_aggs;
   sa.single_band = plan.bands == 1;
+  sa.done_count = reinterpret_cast<unsigned int*>(d + 8);  // zeroed with the ticket
+  sa.done_flag = const_cast<int*>(done);
   cudaStream_t s = c.stream;
   if (!sa.single_band && !cuda_ok(cudaMemsetAsync(d, 0, o_aggs, s), "cudaMemsetAsync")) return true;
   cudaEvent_t* tev = c.timing ? &c.ev[3 * (c.timed_calls % Context::kTimingSlots)] : nullptr;
@@ -769,7 +779,18 @@ bool compress_host_direct(Context& c, int sc, int width, int height, const unsig
     if (!cuda_ok(cudaEventRecord(tev[2], s), "cudaEventRecord")) return true;
     c.timed_calls++;
   }
-  if (!cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return true;
+  bool seen = false;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (unsigned int i = 1;; ++i) {
+    if (*done) {
+      seen = true;
+      break;
+    }
+    if ((i & 1023u) == 0 && std::chrono::steady_clock::now() - t0 > kSmallPollLimit) break;
+  }
+  // the blocks and the timeout flag are read only after the flag was seen
+  std::atomic_thread_fence(std::memory_order_acquire);
+  if (!seen && !cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return true;
   if (*flag) set_error("a bounded wait in the dither scan gave up");
   return true;
 }

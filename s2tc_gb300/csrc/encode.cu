@@ -1517,6 +1517,19 @@ __global__ void __launch_bounds__(kStripThreads, 2) k_strip_quick(const __grid_c
       }
     }
   }
+  if (a.done_flag) {
+    // every thread's blocks are visible system-wide before the last band to
+    // finish raises the flag that the host polls
+    __threadfence_system();
+    __syncthreads();
+    if (t == 0) {
+      const unsigned int prev = a.single_band ? 0u : atomicAdd(a.done_count, 1u);
+      if ((long long)prev + 1 == a.nbands) {
+        __threadfence_system();
+        *reinterpret_cast<volatile int*>(a.done_flag) = 1;
+      }
+    }
+  }
 }
 
 template <int DXT, int REFINE, int SEG>
@@ -1591,6 +1604,7 @@ cudaError_t S2TC_CAT(launch_strip_m, S2TC_METRIC)(StripArgs a, const void* tmap,
              (a.single_band && a.nbands != 1)) {
     return cudaErrorInvalidValue;
   }
+  if (a.done_flag && !a.done_count && !a.single_band) return cudaErrorInvalidValue;
   CUtensorMap map;
   if (a.use_tma) map = *static_cast<const CUtensorMap*>(tmap);
   else std::memset(&map, 0, sizeof(map));

@@ -84,6 +84,10 @@ struct StripArgs {
   int use_tma;          // RGBA8 rows through the tensor map (16-byte aligned source)
   long long tma_rows;   // 256-texel rows the tensor map covers (texels / 256)
   DitherWork scan;      // scan state: status, aggs, ticket (zeroed by the launcher), error
+  // optional: the CTA that finishes last sets *done_flag (host memory) after
+  // every block is written; *done_count (zeroed) counts finished bands
+  unsigned int* done_count;
+  int* done_flag;
 };
 
 // Launches k_strip_quick over a.nbands bands; `scratch` holds
