@@ -655,8 +655,10 @@ __host__ __device__ __forceinline__ RandLayout rand_layout(int m) {
   L.c = align16(L.p + size_t(m) * sizeof(P));          // prepared candidates
   L.a = align16(L.c + size_t(m) * sizeof(uint16_t));   // candidate colours, 5:6:5
   L.d = align16(L.a + size_t(m));                       // candidate alphas
-  L.e = align16(L.d + size_t(m) * kRowBytes);          // colour distance rows
-  L.u = align16(L.e + size_t(m) * 32);                  // alpha rows (16-bit)
+  // the alpha rows (16-bit, 32 bytes each) reuse the colour rows' space: the
+  // alpha search starts after the colour search has read its last row
+  L.e = L.d;
+  L.u = align16(L.d + size_t(m) * kRowBytes);          // colour distance rows
   L.t = align16(L.u + size_t(m) * 2 * sizeof(uint16_t));  // unique colour / alpha indices
   L.bytes = align16(L.t + kDedupWords * sizeof(uint32_t));  // dedup table
   return L;
@@ -943,11 +945,10 @@ __device__ __forceinline__ int dedup(int mm, int lane, int nslots, Slot slot, ui
 }
 
 // CTAs per SM the register budget allows: at 64 random candidates a CTA of
-// four warps holds about 40 KB of shared memory with 16-bit distance rows
-// (five fit an SM) and 53 KB with 32-bit rows (four fit), so the 32-bit
-// metrics get the registers of four CTAs per SM.
+// four warps holds about 30 KB of shared memory with 16-bit distance rows and
+// 43 KB with 32-bit rows, so five CTAs fit an SM either way.
 #ifndef S2TC_RAND_MINBLOCKS
-#define S2TC_RAND_MINBLOCKS (kSmallDist ? 5 : 4)
+#define S2TC_RAND_MINBLOCKS 5
 #endif
 template <int DXT, int REFINE>
 __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode_rand(EncodeWork w, int m) {
