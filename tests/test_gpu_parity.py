@@ -537,6 +537,38 @@ def test_pipelined_host_path(lib):
             assert np.array_equal(a, b), (sc, hex(fmt), dither, metric, nr)
 
 
+def test_pipelined_host_path_pinned(lib):
+    """The pipelined tx_compress_dxtn with pinned source and destination: the
+    blocks come back chunk by chunk on the download stream while later
+    chunks are encoded on four streams (the doubling dither ranges of a
+    2052x2050 image: 16, 32, 64 and 141 tiles; chunks of at most 33 block
+    rows), packed or with padded rows (two-dimensional copies), and the DXT5
+    all-texels search's carried endpoint crosses from the last chunk to the
+    next call's first.  Bytes equal the device API's."""
+    torch = pytest.importorskip("torch")
+    w, h = 2052, 2050
+    for sc, fmt, dither, metric, nr, refine, stride in ((4, 0x83F3, 1, 3, 0, 2, 0), (4, 0x83F3, 1, 5, 0, 1, 9000),
+                                                         (3, 0x83F1, 1, 5, -1, 1, 0), (4, 0x83F1, 1, 5, -1, 1, 8300)):
+        img = workloads.value_noise_rgba(70 + sc, w, h)[:, :, :sc].copy().reshape(-1)
+        bs = 8 if fmt == 0x83F1 else 16
+        row = ((w + 3) // 4) * bs
+        rows = (h + 3) // 4
+        h_src = torch.from_numpy(img).pin_memory()
+        h_dst = torch.zeros(rows * (stride or row), dtype=torch.uint8).pin_memory()
+        s2.set_env(dither, metric, nr, refine)
+        opt = s2.options(dither, metric, nr, refine)
+        d_src = torch.from_numpy(img).cuda()
+        d_dst = torch.zeros(row * rows, dtype=torch.uint8, device="cuda")
+        for _ in range(2):  # the second call reads the first one's carried endpoint
+            lib.tx_compress_dxtn(sc, w, h, h_src.data_ptr(), fmt, h_dst.data_ptr(), stride)
+            s2.gpu_compress(sc, w, h, d_src, fmt, d_dst, opt=opt)
+            s2.gpu_synchronize(None)
+            got = h_dst.numpy()
+            if stride:
+                got = got.reshape(rows, stride)[:, :row].reshape(-1)
+            assert np.array_equal(got, d_dst.cpu().numpy()), (sc, hex(fmt), metric, stride)
+
+
 # --------------------------------------------------------------- strip kernel
 # The quick mode with NONE or SIMPLE dither runs as one fused kernel over
 # bands of whole block rows (images up to 4160 texels wide): the scan's
