@@ -800,16 +800,19 @@ bool compress_host_small(Context& c, int sc, int width, int height, const unsign
   *done = false;
   const long long npx = (long long)width * height;
   StripPlan plan;
-  if (npx > kSmallCallTexels || !strip_mode(opt, width, height, &plan)) return false;
-  *done = true;
+  if (npx >= kPipeMinTexels || !strip_mode(opt, width, height, &plan)) return false;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
   const size_t row_bytes = size_t(bw) * bs, out_bytes = row_bytes * bh;
   {
     const long long diff =
         dstRowStride >= width * (bs / 4) ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs / 4) : 0;
-    if (c.pageable_access == 1 && diff >= 0)
+    if (c.pageable_access == 1 && diff >= 0) {
+      *done = true;
       return compress_host_direct(c, sc, width, height, src, dxt, dest, diff, opt, plan);
+    }
   }
+  if (npx > kSmallCallTexels) return false;
+  *done = true;
   const size_t o_ticket = align_up(size_t(npx) * sc, 256), o_status = o_ticket + 16;
   const size_t o_flag = align_up(o_status + size_t(plan.bands) * 8, 16), o_blocks = o_flag + 16;
   const size_t o_aggs = align_up(o_blocks + out_bytes, 16), total = o_aggs + size_t(plan.bands) * 72;
