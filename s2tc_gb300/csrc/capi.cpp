@@ -723,8 +723,9 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
   return true;
 }
 
-// Small images in the quick mode: one fused launch between one upload and one
-// download.  A device arena holds [pixels | ticket | status words | flag |
+// Quick-mode images where the device reads host memory coherently, of any
+// size: compress_host_direct (below).  Elsewhere, small images in the quick
+// mode: one fused launch between one upload and one download.  A device arena holds [pixels | ticket | status words | flag |
 // blocks | aggregate records] and a pinned buffer mirrors its first part:
 // the upload carries the pixels and the zeroed ticket, status words and
 // timeout flag, the download brings back the flag and the blocks.  Four CUDA
@@ -744,8 +745,17 @@ constexpr long long kSmallCallTexels = 1ll << 16;
 // writes the rows in order.  The wait is a poll of a flag in pinned memory
 // that the last band to finish raises after its blocks (bounded: past
 // kSmallPollLimit the stream wait takes over), which returns sooner than the
-// stream wait.
+// stream wait.  The bands read the pixels over the host link as they need
+// them, so the link's time overlaps the scan and the encoding without ranges:
+// a 1024^2 call took 60.7 µs against 96.6 µs through an upload and a
+// download, a 4096^2 call 0.425 ms against 0.450 ms for the pipelined ranges.
 constexpr auto kSmallPollLimit = std::chrono::milliseconds(5);
+
+// S2TC_HOST_DIRECT=0 keeps such calls on the staged and pipelined paths.
+bool host_direct_enabled() {
+  const char* v = std::getenv("S2TC_HOST_DIRECT");
+  return !(v && v[0] == '0');
+}
 bool compress_host_direct(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                           unsigned char* dest, long long diff, const s2tc_options& opt, const StripPlan& plan) {
   const int bw = (width + 3) / 4, bs = block_bytes(dxt);
@@ -800,13 +810,13 @@ bool compress_host_small(Context& c, int sc, int width, int height, const unsign
   *done = false;
   const long long npx = (long long)width * height;
   StripPlan plan;
-  if (npx >= kPipeMinTexels || !strip_mode(opt, width, height, &plan)) return false;
+  if (!strip_mode(opt, width, height, &plan)) return false;
   const int bw = (width + 3) / 4, bh = (height + 3) / 4, bs = block_bytes(dxt);
   const size_t row_bytes = size_t(bw) * bs, out_bytes = row_bytes * bh;
   {
     const long long diff =
         dstRowStride >= width * (bs / 4) ? (long long)dstRowStride - (long long)((width + 3) & ~3) * (bs / 4) : 0;
-    if (c.pageable_access == 1 && diff >= 0) {
+    if (c.pageable_access == 1 && diff >= 0 && host_direct_enabled()) {
       *done = true;
       return compress_host_direct(c, sc, width, height, src, dxt, dest, diff, opt, plan);
     }

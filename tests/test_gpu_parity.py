@@ -579,11 +579,15 @@ STRIP_SHAPES = [(3, 5), (255, 1), (257, 3), (1000, 77), (1001, 70), (4160, 9), (
                 (1089, 301), (2000, 600), (64, 260), (130, 131), (4160, 1201), (1024, 1024)]
 
 
+@pytest.mark.parametrize("direct", ["1", "0"])
 @pytest.mark.parametrize("fmt", [0x83F1, 0x83F2, 0x83F3])
-def test_strip_bands_and_edges(lib, oracle, fmt):
+def test_strip_bands_and_edges(lib, oracle, monkeypatch, fmt, direct):
     """Widths around the band sizes, the 17- and 65-texel segments and the
     4160 limit (4161 takes the two kernels), widths and heights that are not multiples of 4, RGB and RGBA,
-    NONE and SIMPLE dither, every refinement, against the oracle."""
+    NONE and SIMPLE dither, every refinement, against the oracle; with the
+    kernel reading the caller's host memory where it can (direct), and
+    through the staging copies (S2TC_HOST_DIRECT=0)."""
+    monkeypatch.setenv("S2TC_HOST_DIRECT", direct)
     rng = np.random.default_rng(fmt)
     for k, (w, h) in enumerate(STRIP_SHAPES):
         sc = 4 if k % 2 == 0 else 3
@@ -615,10 +619,15 @@ def test_strip_device_sources(lib, oracle):
             assert np.array_equal(got, want), (w, h, hex(fmt), shift)
 
 
-def test_strip_pipelined_host_path(lib, oracle):
-    """tx_compress_dxtn on images of at least 4 Mi texels in quick mode: the
-    image goes up in ranges of bands and each range is one fused launch whose
-    look-back reaches into the ranges before it."""
+@pytest.mark.parametrize("direct", ["1", "0"])
+def test_strip_pipelined_host_path(lib, oracle, monkeypatch, direct):
+    """tx_compress_dxtn on images of at least 4 Mi texels in quick mode: where
+    the GPU reads host memory coherently, one fused launch reads the pixels
+    and writes the blocks in host memory (direct); otherwise
+    (S2TC_HOST_DIRECT=0 here) the image goes up in ranges of bands and each
+    range is one fused launch whose look-back reaches into the ranges before
+    it."""
+    monkeypatch.setenv("S2TC_HOST_DIRECT", direct)
     for w, h, fmt, sc, dither in ((2048, 2051, 0x83F1, 4, 1), (8192, 515, 0x83F3, 4, 1), (3001, 1500, 0x83F2, 3, 0)):
         img = workloads.plain_rgba(22, w, h)[:, :, :sc].reshape(-1) if sc == 4 else \
             np.ascontiguousarray(workloads.plain_rgba(22, w, h)[:, :, :3]).reshape(-1)

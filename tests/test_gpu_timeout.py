@@ -45,13 +45,14 @@ def test_device_call_reports_timeout_then_recovers(lib, oracle):
 
 @pytest.mark.parametrize("nrandom,w,hold", [(-1, 4096, 300), (0, 2048, 30)])
 def test_pipelined_host_call_reports_timeout_then_recovers(lib, oracle, nrandom, w, hold):
-    """tx_compress_dxtn on the two pipelined paths: the image goes up range by
-    range and each range is scanned as it lands.  The quick mode (nrandom -1,
-    4096x2048) runs the fused strip kernel over 512 bands of one block row in
-    two ranges of 256; the all-texel search (nrandom 0, 2048x2048) runs the
-    dither over 253 tiles of 16640 texels in ranges of 16, 32, 64 and 141.
-    The held band or tile sits in the second range, so waits across a range
-    boundary give up too."""
+    """tx_compress_dxtn on the large-image paths.  The quick mode (nrandom -1,
+    4096x2048) runs the fused strip kernel over 512 bands of one block row:
+    in one launch that reads host memory where the GPU reads it coherently,
+    else in two ranges of 256 as the image goes up; the all-texel search
+    (nrandom 0, 2048x2048) runs the dither over 253 tiles of 16640 texels in
+    ranges of 16, 32, 64 and 141 as the image goes up.  The held band or tile
+    sits in the second half or range, so waits across a range boundary give
+    up too."""
     h, fmt = 2048, 0x83F1
     img = workloads.plain_rgba(10, w, h).reshape(-1)
     s2.set_env(1, s2.WAVG, nrandom, 1)
