@@ -36,7 +36,10 @@
 namespace s2tc {
 namespace {
 
-constexpr int kThreads = 256;
+#ifndef S2TC_DITHER_THREADS
+#define S2TC_DITHER_THREADS 256
+#endif
+constexpr int kThreads = S2TC_DITHER_THREADS;
 constexpr int kSeg = 65;                // texels per thread (odd: conflict-free)
 constexpr int kTile = kThreads * kSeg;  // 16640 texels per tile
 using TileSmem = ScanSmem<kThreads, kSeg>;
