@@ -457,6 +457,29 @@ int check_error_flag(Context& c, cudaStream_t s) {
   return take_flag(c);
 }
 
+// The same when the flag's read-back is the last thing the call's work needs
+// (every copy and kernel of the call is ordered before it on `s`): the host
+// polls the pinned word that the read-back overwrites, which returns sooner
+// than the stream wait; past kFlagPollLimit the stream wait takes over.
+constexpr auto kFlagPollLimit = std::chrono::milliseconds(20);
+int finish_polled(Context& c, cudaStream_t s) {
+  volatile int* hf = static_cast<volatile int*>(c.host_flag.p);
+  *hf = -1;  // the read-back writes 0 or 1
+  if (!enqueue_flag(c, s)) return ST_CUDA_ERROR;
+  bool seen = false;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (unsigned int i = 1;; ++i) {
+    if (*hf != -1) {
+      seen = true;
+      break;
+    }
+    if ((i & 1023u) == 0 && std::chrono::steady_clock::now() - t0 > kFlagPollLimit) break;
+  }
+  std::atomic_thread_fence(std::memory_order_acquire);
+  if (!seen && !cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize")) return ST_CUDA_ERROR;
+  return take_flag(c);
+}
+
 bool host_pinned(const void* p) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -581,7 +604,7 @@ bool compress_host_pipelined_strip(Context& c, int sc, int width, int height, co
       !cuda_ok(cudaStreamWaitEvent(s, c.pipe_out[0], 0), "cudaStreamWaitEvent") ||
       !cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord"))
     return true;
-  check_error_flag(c, s);
+  finish_polled(c, s);
   return true;
 }
 
@@ -719,7 +742,7 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
       !cuda_ok(cudaStreamWaitEvent(s, c.pipe_out[0], 0), "cudaStreamWaitEvent") ||
       !cuda_ok(cudaEventRecord(c.arena_free, s), "cudaEventRecord"))
     return true;
-  check_error_flag(c, s);
+  finish_polled(c, s);
   return true;
 }
 
