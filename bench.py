@@ -1255,15 +1255,22 @@ def main() -> None:
         for i in range(min(args.warmup, 3)):
             lib.tx_compress_dxtn(sc, w, h, h_src[i % NIMG].data_ptr(), fmt, h_dst.data_ptr(), 0)
         barrier()
+        call_s = []
         t0 = time.perf_counter()
         for i in range(args.steps):
+            c0 = time.perf_counter()
             lib.tx_compress_dxtn(sc, w, h, h_src[i % NIMG].data_ptr(), fmt, h_dst.data_ptr(), 0)
+            call_s.append(time.perf_counter() - c0)
         t_e2e = time.perf_counter() - t0
         barrier()
         t_e2e, e2e_value = aggregate_ranks(t_e2e, args.steps * npx, dist, "cuda")
         e2e = {"value": e2e_value, "unit": "texels/s",
                "h2d_bytes_per_step": npx * sc, "d2h_bytes_per_step": out_bytes,
-               "ms_per_step": 1000 * t_e2e / args.steps}
+               "ms_per_step": 1000 * t_e2e / args.steps,
+               # the spread of the synchronous calls (this rank): the value above
+               # is the mean; a slow call on a busy host shows up here
+               "ms_per_call_median": 1000 * float(np.median(call_s)),
+               "ms_per_call_max": 1000 * float(np.max(call_s))}
 
     # --- roofline of the dominant kernel
     peaks = {}
