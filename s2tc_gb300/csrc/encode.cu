@@ -640,8 +640,12 @@ constexpr int kRowBytes = kSmallDist ? 32 : 64;
 // Candidates are deduplicated through a per-warp table indexed by the value
 // inside the block's bounding box when the box has at most kDedupSlots
 // values (first occurrence and first repeat per value).
-constexpr int kDedupSlots = 512;
+#ifndef S2TC_DEDUP_SLOTS
+#define S2TC_DEDUP_SLOTS 256
+#endif
+constexpr int kDedupSlots = S2TC_DEDUP_SLOTS;
 constexpr int kDedupWords = 2 * kDedupSlots;
+static_assert(kDedupSlots >= 256, "the alpha search indexes the table by the 256 alpha values");
 
 struct RandLayout {
   size_t p, c, a, d, e, u, t, bytes;  // section offsets and bytes per warp
@@ -945,11 +949,12 @@ __device__ __forceinline__ int dedup(int mm, int lane, int nslots, Slot slot, ui
 }
 
 // CTAs per SM the register budget allows: at 64 random candidates a CTA of
-// four warps holds about 30 KB of shared memory with 16-bit distance rows
-// (seven fit an SM: 72 registers, measured 5% faster than five on the mip
-// chains) and 43 KB with 32-bit rows (five fit: 96 registers).
+// four warps holds about 22 KB of shared memory with 16-bit distance rows
+// (seven CTAs: 72 registers, measured 5% faster than five on the mip chains)
+// and 35 KB with 32-bit rows (six CTAs: 80 registers and a few spilled words,
+// 1.4% faster than five on a normal map).
 #ifndef S2TC_RAND_MINBLOCKS
-#define S2TC_RAND_MINBLOCKS (kSmallDist ? 7 : 5)
+#define S2TC_RAND_MINBLOCKS (kSmallDist ? 7 : 6)
 #endif
 template <int DXT, int REFINE>
 __global__ void __launch_bounds__(32 * kRandWarps, S2TC_RAND_MINBLOCKS) k_encode_rand(EncodeWork w, int m) {
