@@ -748,8 +748,9 @@ bool compress_host_pipelined(Context& c, int sc, int width, int height, const un
 
 // Quick-mode images where the device reads host memory coherently, of any
 // size: compress_host_direct (below).  Elsewhere, small images in the quick
-// mode: one fused launch between one upload and one download.  A device arena holds [pixels | ticket | status words | flag |
-// blocks | aggregate records] and a pinned buffer mirrors its first part:
+// mode: one fused launch between one upload and one download.  A device
+// arena holds [pixels | ticket | status words | flag | blocks | aggregate
+// records] and a pinned buffer mirrors its first part:
 // the upload carries the pixels and the zeroed ticket, status words and
 // timeout flag, the download brings back the flag and the blocks.  Four CUDA
 // calls per image (upload, launch, download, wait) instead of about ten: a
@@ -764,7 +765,7 @@ constexpr long long kSmallCallTexels = 1ll << 16;
 // caller's pixels and writes the caller's blocks itself: the call is one
 // launch and one wait (plus one memset of the scan state when the image has
 // more than one band), with no staging copies.  Overlapping output rows (a
-// dstRowStride below the padded row) keep the staging path, whose host copy
+// dstRowStride below the padded row) keep the copying paths, whose host copy
 // writes the rows in order.  The wait is a poll of a flag in pinned memory
 // that the last band to finish raises after its blocks (bounded: past
 // kSmallPollLimit the stream wait takes over), which returns sooner than the
@@ -779,6 +780,7 @@ bool host_direct_enabled() {
   const char* v = std::getenv("S2TC_HOST_DIRECT");
   return !(v && v[0] == '0');
 }
+
 bool compress_host_direct(Context& c, int sc, int width, int height, const unsigned char* src, int dxt,
                           unsigned char* dest, long long diff, const s2tc_options& opt, const StripPlan& plan) {
   const int bw = (width + 3) / 4, bs = block_bytes(dxt);
